@@ -1,0 +1,197 @@
+/*
+ * mcrt_gb300.h -- C ABI of the GB300 (sm_103a) path-tracing library.
+ *
+ * Plain C: pointers, sizes and status codes; no C++ or torch types.  Every entry
+ * point returns MCRT_OK (0) or a negative MCRT_ERR_* code and never throws across
+ * the boundary; mcrt_last_error() returns the message of the calling thread's last
+ * failure.  Device memory for a scene is owned by the library; the caller owns all
+ * buffers it passes in.  A scene handle may be used from several host threads as
+ * long as each thread uses its own CUDA stream.
+ *
+ * Reference interfaces replaced (paths are relative to the MCRT source tree):
+ *   SceneBVH::SceneBVH            src/core/scenebvh.h:14, scenebvh.cpp:404-444 -> mcrt_scene_create
+ *   SceneBVH::intersect           src/core/scenebvh.h:17, scenebvh.cpp:353-377 -> mcrt_trace_closest
+ *   SceneBVH::occluded            src/core/scenebvh.h:18, scenebvh.cpp:379-396 -> mcrt_trace_any
+ *   SceneBVH::~SceneBVH           src/core/scenebvh.cpp:398-402                -> mcrt_scene_destroy
+ *   rayTrace + DemoSimple::run    src/examples/pt/demo_pt.cpp:512-720        -> mcrt_render
+ *   (no reference counterpart: path-replay adjoint, batched launch)           -> mcrt_render_adjoint,
+ *                                                                                mcrt_render_batch
+ */
+#ifndef MCRT_GB300_H
+#define MCRT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCRT_ABI_VERSION 1
+
+/* status codes */
+#define MCRT_OK 0
+#define MCRT_ERR_INVALID_ARGUMENT (-1)
+#define MCRT_ERR_CUDA (-2)
+#define MCRT_ERR_OUT_OF_MEMORY (-3)
+#define MCRT_ERR_QUEUE_OVERFLOW (-4)
+#define MCRT_ERR_STACK_OVERFLOW (-5)
+#define MCRT_ERR_INTERNAL (-6)
+#define MCRT_ERR_IO (-7)
+
+/* material types: the values of MaterialType in src/core/material.h:7, plus GGX */
+#define MCRT_MAT_LGHT 0 /* emitter: radiance = color (Scene::lightRadiance, scene.cpp:345-366) */
+#define MCRT_MAT_DIFF 1 /* Lambert (bsdf.cpp:51-116) */
+#define MCRT_MAT_SPEC 2 /* mirror (bsdf.cpp:134-191) */
+#define MCRT_MAT_REFR 3 /* smooth dielectric, exact Fresnel (bsdf.cpp:319-440) */
+#define MCRT_MAT_GLSY 4 /* Phong lobe, exponent 25 (bsdf.cpp:209-301) */
+#define MCRT_MAT_GGX 8  /* GGX conductor (new: Walter 2007, Heitz 2018, Schlick F0 = color) */
+
+typedef struct mcrt_material {
+    int32_t type;           /* MCRT_MAT_* */
+    float   color[3];       /* albedo / F0 / transmission tint / emitted radiance */
+    float   roughness;      /* GGX alpha */
+    float   ior;            /* REFR index of refraction (reference: fixed 1.33) */
+    int32_t albedo_param;   /* adjoint parameter group of a DIFF albedo, -1 = none */
+    int32_t emission_param; /* adjoint parameter group of an LGHT radiance, -1 = none */
+} mcrt_material;
+
+/* A binary BVH given by the caller (e.g. the reference SplitBVH tree,
+ * splitbvh.h:32-58): node i is a leaf when node_info[6i] == 1.
+ *   node_box[6i..6i+5]  = min xyz, max xyz of the node's bounding_box
+ *   node_info[6i..6i+5] = is_leaf, left, right, split_axis, ref_begin, ref_count
+ *   refs: ref_prim[k] primitive id, ref_box[6k..] its clipped bound
+ * Children are visited left-first iff ray.dir[split_axis] > 0 (splitbvh.cpp:75). */
+typedef struct mcrt_bvh_tree {
+    int32_t        num_nodes;
+    int32_t        num_refs;
+    const float*   node_box;
+    const int32_t* node_info;
+    const int32_t* ref_prim;
+    const float*   ref_box;
+} mcrt_bvh_tree;
+
+#define MCRT_BUILD_SAH 0      /* the library's own binned-SAH builder */
+#define MCRT_BUILD_EXTERNAL 1 /* use desc->external_tree */
+
+typedef struct mcrt_scene_desc {
+    int64_t              num_triangles;
+    const float*         vertices;     /* [num_triangles][3][3] a, b, c (TriangleObject::a,b,c) */
+    const float*         normals;      /* [num_triangles][3][3] na, nb, nc; NULL -> face normal */
+    const int32_t*       material_ids; /* [num_triangles] */
+    int32_t              num_materials;
+    const mcrt_material* materials;
+    int32_t              env_width; /* 0 -> no environment map */
+    int32_t              env_height;
+    const float*         env_rgb; /* [env_height][env_width][3], row-major, top row first (envmap.h:20-25) */
+    int32_t              builder; /* MCRT_BUILD_* */
+    int32_t              leaf_size; /* own builder: max triangles per leaf (0 -> 4) */
+    const mcrt_bvh_tree* external_tree;
+} mcrt_scene_desc;
+
+typedef struct mcrt_scene mcrt_scene;
+
+/* Rays and hits are structure-of-arrays-of-float4, 32 B per ray:
+ *   rays[2i]   = {ox, oy, oz, tmin}, rays[2i+1] = {dx, dy, dz, tmax}
+ * Hits: 16 B per ray {t, u, v, prim as int bits}; prim = -1 on a miss. */
+typedef struct mcrt_ray {
+    float org[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} mcrt_ray;
+
+typedef struct mcrt_hit {
+    float   t;
+    float   u;
+    float   v;
+    int32_t prim;
+} mcrt_hit;
+
+/* traversal modes */
+#define MCRT_TRAVERSE_FAST 0 /* 64-B two-child nodes, watertight FP32 test (Woop et al. 2013)
+                                with the reference's absolute |det| < 1e-6 rejection */
+#define MCRT_TRAVERSE_REF 1  /* the reference's own order and arithmetic: per-node box test at
+                                visit time, clipped-bound test, Moller-Trumbore, inv_dir = 0
+                                for zero direction components; bit-identical hits */
+
+/* pointer-location flags for mcrt_trace_* and mcrt_render* */
+#define MCRT_PTR_HOST 0   /* buffers are host memory: copied in/out inside the call */
+#define MCRT_PTR_DEVICE 1 /* buffers are device memory */
+
+typedef struct mcrt_camera {
+    float   origin[3];
+    float   target[3];
+    float   up[3]; /* Scene::setCamera passes (0, 1, 0) */
+    float   fov_y; /* degrees */
+    int32_t width;
+    int32_t height;
+} mcrt_camera;
+
+typedef struct mcrt_render_params {
+    int32_t  spp;
+    int32_t  max_depth;   /* bounces n = 0..max_depth, as demo_pt.cpp:520-523 */
+    int32_t  rr_depth;    /* Russian roulette from this vertex index, -1 = off */
+    uint64_t seed;
+    int32_t  traverse;    /* MCRT_TRAVERSE_* for every ray of the render */
+    int32_t  ptr_mode;    /* MCRT_PTR_* for image / gradient buffers */
+    int64_t  path_chunk;  /* paths in flight per wave, 0 -> library default */
+    int32_t  block_size;  /* threads per block of the wavefront kernels, 0 -> default */
+    int32_t  use_graph;   /* capture each wave's per-stage kernels in a CUDA graph */
+} mcrt_render_params;
+
+typedef struct mcrt_render_stats {
+    int64_t paths;
+    int64_t extension_rays;
+    int64_t shadow_rays;
+    int32_t waves;
+    int32_t kernel_launches;
+    float   device_ms; /* CUDA-event time of the kernels (excludes host copies) */
+} mcrt_render_stats;
+
+int         mcrt_get_abi_version(void);
+const char* mcrt_last_error(void);
+
+/* Builds the BVH on the host (own SAH builder or the given tree), flattens it, builds
+ * the emitter and environment-map sampling tables and uploads everything. */
+int mcrt_scene_create(const mcrt_scene_desc* desc, mcrt_scene** out_scene);
+int mcrt_scene_destroy(mcrt_scene* scene);
+/* Replace material colours (e.g. optimised albedos) without rebuilding the scene. */
+int mcrt_scene_set_materials(mcrt_scene* scene, int32_t num_materials, const mcrt_material* materials,
+                             void* stream);
+/* Sizes of the device-resident scene: fast nodes, reference-layout nodes, triangle refs. */
+int mcrt_scene_info(const mcrt_scene* scene, int64_t* fast_nodes, int64_t* ref_nodes, int64_t* refs,
+                    int64_t* device_bytes);
+
+/* Closest hit for n rays: SceneBVH::intersect / SplitBVH::intersect semantics with the
+ * caller's [tmin, tmax]; ties keep the first hit in traversal order. */
+int mcrt_trace_closest(mcrt_scene* scene, const mcrt_ray* rays, int64_t n, mcrt_hit* hits, int32_t traverse,
+                       int32_t ptr_mode, void* stream);
+/* Any hit: occluded[i] = 1 when some triangle is hit with tmin < t < tmax. */
+int mcrt_trace_any(mcrt_scene* scene, const mcrt_ray* rays, int64_t n, int32_t* occluded, int32_t traverse,
+                   int32_t ptr_mode, void* stream);
+
+/* Forward render: rgb_out[height][width][3] = per-pixel mean of the clamped per-sample
+ * radiance (row 0 = the camera's bottom row, as FrameBuffer::accumulatePixel). */
+int mcrt_render(mcrt_scene* scene, const mcrt_camera* camera, const mcrt_render_params* params, float* rgb_out,
+                mcrt_render_stats* stats, void* stream);
+
+/* Path-replay adjoint of mcrt_render (same camera/params/seed): given dL/dimage
+ * [height][width][3], ADDS dL/d(albedo) [num_albedo_params][3] and
+ * dL/d(emission) [num_emission_params][3]; the caller zeroes them.  Memory is
+ * O(pixels + parameters): paths are replayed from their seeds, nothing is taped. */
+int mcrt_render_adjoint(mcrt_scene* scene, const mcrt_camera* camera, const mcrt_render_params* params,
+                        const float* dL_dimage, float* d_albedo, int32_t num_albedo_params, float* d_emission,
+                        int32_t num_emission_params, mcrt_render_stats* stats, void* stream);
+
+/* Many (scene, camera, params) jobs of uneven size in one wavefront: jobs share every
+ * stage launch.  rgb_out[j] receives job j's image. */
+int mcrt_render_batch(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cameras,
+                      const mcrt_render_params* params, float* const* rgb_out, mcrt_render_stats* stats,
+                      void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCRT_GB300_H */

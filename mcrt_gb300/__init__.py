@@ -1,0 +1,20 @@
+"""mcrt_gb300: GB300-native (sm_103a) wavefront path tracer behind MCRT's scene API.
+
+Public surface:
+  SceneDesc, Material, CameraDesc      host-side scene description (scene.py)
+  GpuScene                             device scene: trace_closest / trace_any / render /
+                                       render_adjoint / set_materials
+  render_batch                         many scenes/cameras/spp budgets in one wavefront
+  build()                              compile the in-tree native library
+The native library (mcrt_gb300/_lib/libmcrt_gb300.so, C ABI in include/mcrt_gb300.h)
+is required: there is no CPU fallback.
+"""
+from . import scenes
+from ._native import (PTR_DEVICE, PTR_HOST, TRAVERSE_FAST, TRAVERSE_REF, McrtError, load)
+from .native_build import build
+from .scene import (DIFF, GGX, GLSY, LGHT, REFR, SPEC, CameraDesc, GpuScene, Material, SceneDesc, make_params,
+                    render_batch)
+
+__all__ = ["SceneDesc", "Material", "CameraDesc", "GpuScene", "render_batch", "build", "load", "scenes",
+           "McrtError", "TRAVERSE_FAST", "TRAVERSE_REF", "PTR_HOST", "PTR_DEVICE", "make_params",
+           "LGHT", "DIFF", "SPEC", "REFR", "GLSY", "GGX"]

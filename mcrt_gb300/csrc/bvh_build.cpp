@@ -1,0 +1,238 @@
+// Binned-SAH BVH builder (host, multithreaded).
+//
+// The reference builds a spatial-split BVH (splitbvh.cpp:1410-1625) with a serial,
+// shared_ptr-per-node recursion: 58 s for 1.3 M triangles.  This builder makes the
+// trees the GPU traverses: object splits chosen by the surface-area heuristic over
+// 32 centroid bins per axis (MacDonald & Booth 1990; binning after Wald 2007),
+// leaves of at most `leaf_size` triangles, subtrees built in parallel.  A reference
+// tree can be supplied instead through mcrt_scene_desc::external_tree.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <future>
+#include <limits>
+#include <thread>
+
+#include "host.h"
+
+namespace mcrt {
+namespace {
+
+constexpr int kBins = 32;
+
+struct Box
+{
+    float lo[3], hi[3];
+    Box() { reset(); }
+    void reset()
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            lo[k] = std::numeric_limits<float>::infinity();
+            hi[k] = -std::numeric_limits<float>::infinity();
+        }
+    }
+    void grow(const Box& b)
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            lo[k] = std::min(lo[k], b.lo[k]);
+            hi[k] = std::max(hi[k], b.hi[k]);
+        }
+    }
+    void grow(const float* p)
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            lo[k] = std::min(lo[k], p[k]);
+            hi[k] = std::max(hi[k], p[k]);
+        }
+    }
+    double half_area() const
+    {
+        if (!(hi[0] >= lo[0])) return 0.0;
+        double dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        return dx * dy + dy * dz + dz * dx;
+    }
+};
+
+struct Builder
+{
+    const std::vector<Box>&   boxes;
+    const std::vector<float>& cen;  // 3 per prim
+    std::vector<int32_t>&     prims;
+    int                       leaf_size;
+    // node storage, preallocated (a binary tree over n >= 1 leaves has < 2n nodes)
+    std::vector<Box>         nbox;
+    std::vector<int32_t>     ninfo;  // 6 per node
+    std::atomic<int>         next_node{0};
+    std::atomic<int>         threads_left{0};
+
+    Builder(const std::vector<Box>& b, const std::vector<float>& c, std::vector<int32_t>& p, int leaf)
+        : boxes(b), cen(c), prims(p), leaf_size(leaf)
+    {
+        size_t cap = 2 * p.size() + 1;
+        nbox.resize(cap);
+        ninfo.resize(6 * cap);
+    }
+
+    int alloc() { return next_node.fetch_add(1); }
+
+    void make_leaf(int node, int begin, int end)
+    {
+        int32_t* info = &ninfo[6 * node];
+        info[0] = 1;
+        info[1] = info[2] = -1;
+        info[3] = 0;
+        info[4] = begin;
+        info[5] = end - begin;
+    }
+
+    void build(int node, int begin, int end)
+    {
+        Box bb, cb;
+        for (int i = begin; i < end; ++i)
+        {
+            int p = prims[i];
+            bb.grow(boxes[p]);
+            cb.grow(&cen[3 * p]);
+        }
+        nbox[node] = bb;
+        int count = end - begin;
+        if (count <= leaf_size)
+        {
+            make_leaf(node, begin, end);
+            return;
+        }
+        // SAH sweep over kBins bins per axis
+        double best = std::numeric_limits<double>::infinity();
+        int    best_axis = -1, best_bin = -1;
+        for (int ax = 0; ax < 3; ++ax)
+        {
+            float ext = cb.hi[ax] - cb.lo[ax];
+            if (!(ext > 0.f)) continue;
+            float scale = kBins / ext;
+            Box   bin_box[kBins];
+            int   bin_cnt[kBins] = {0};
+            for (int i = begin; i < end; ++i)
+            {
+                int p = prims[i];
+                int b = std::min(kBins - 1, static_cast<int>((cen[3 * p + ax] - cb.lo[ax]) * scale));
+                bin_cnt[b]++;
+                bin_box[b].grow(boxes[p]);
+            }
+            double right_area[kBins];
+            int    right_cnt[kBins];
+            Box    acc;
+            int    c = 0;
+            for (int b = kBins - 1; b > 0; --b)
+            {
+                acc.grow(bin_box[b]);
+                c += bin_cnt[b];
+                right_area[b] = acc.half_area();
+                right_cnt[b] = c;
+            }
+            acc.reset();
+            c = 0;
+            for (int b = 0; b < kBins - 1; ++b)
+            {
+                acc.grow(bin_box[b]);
+                c += bin_cnt[b];
+                if (c == 0 || right_cnt[b + 1] == 0) continue;
+                double cost = acc.half_area() * c + right_area[b + 1] * right_cnt[b + 1];
+                if (cost < best)
+                {
+                    best = cost;
+                    best_axis = ax;
+                    best_bin = b;
+                }
+            }
+        }
+        int mid;
+        if (best_axis < 0)
+        {
+            mid = begin + count / 2;  // coincident centroids: split the run in half
+        }
+        else
+        {
+            float ext = cb.hi[best_axis] - cb.lo[best_axis];
+            float scale = kBins / ext;
+            float lo = cb.lo[best_axis];
+            int*  m = std::partition(prims.data() + begin, prims.data() + end, [&](int p) {
+                int b = std::min(kBins - 1, static_cast<int>((cen[3 * p + best_axis] - lo) * scale));
+                return b <= best_bin;
+            });
+            mid = static_cast<int>(m - prims.data());
+            if (mid == begin || mid == end) mid = begin + count / 2;
+        }
+        int left = alloc(), right = alloc();
+        int32_t* info = &ninfo[6 * node];
+        info[0] = 0;
+        info[1] = left;
+        info[2] = right;
+        info[3] = best_axis < 0 ? 0 : best_axis;
+        info[4] = 0;
+        info[5] = 0;
+        const int par_threshold = 16384;
+        if (count > par_threshold && threads_left.fetch_sub(1) > 0)
+        {
+            auto fut = std::async(std::launch::async, [this, left, begin, mid]() { build(left, begin, mid); });
+            build(right, mid, end);
+            fut.get();
+        }
+        else
+        {
+            build(left, begin, mid);
+            build(right, mid, end);
+        }
+    }
+};
+
+}  // namespace
+
+void build_sah_tree(const float* v, int64_t n, int leaf_size, BinaryTree& out)
+{
+    if (leaf_size <= 0) leaf_size = 4;
+    std::vector<Box>     boxes(n);
+    std::vector<float>   cen(3 * n);
+    std::vector<int32_t> prims(n);
+    for (int64_t i = 0; i < n; ++i)
+    {
+        Box b;
+        b.grow(v + 9 * i);
+        b.grow(v + 9 * i + 3);
+        b.grow(v + 9 * i + 6);
+        boxes[i] = b;
+        for (int k = 0; k < 3; ++k) cen[3 * i + k] = 0.5f * (b.lo[k] + b.hi[k]);
+        prims[i] = static_cast<int32_t>(i);
+    }
+    Builder bld(boxes, cen, prims, leaf_size);
+    unsigned hw = std::thread::hardware_concurrency();
+    bld.threads_left = static_cast<int>(hw ? 2 * hw : 8);
+    int root = bld.alloc();
+    if (n > 0) bld.build(root, 0, static_cast<int>(n));
+    int num_nodes = bld.next_node.load();
+    out.node_box.resize(6 * static_cast<size_t>(num_nodes));
+    out.node_info.assign(bld.ninfo.begin(), bld.ninfo.begin() + 6 * static_cast<size_t>(num_nodes));
+    for (int i = 0; i < num_nodes; ++i)
+        for (int k = 0; k < 3; ++k)
+        {
+            out.node_box[6 * i + k] = bld.nbox[i].lo[k];
+            out.node_box[6 * i + 3 + k] = bld.nbox[i].hi[k];
+        }
+    out.ref_prim = prims;
+    out.ref_box.resize(6 * static_cast<size_t>(n));
+    for (int64_t r = 0; r < n; ++r)
+    {
+        const Box& b = boxes[prims[r]];
+        for (int k = 0; k < 3; ++k)
+        {
+            out.ref_box[6 * r + k] = b.lo[k];
+            out.ref_box[6 * r + 3 + k] = b.hi[k];
+        }
+    }
+    out.root = root;
+}
+
+}  // namespace mcrt

@@ -1,0 +1,774 @@
+// Device functions shared by every kernel: vector math, the per-path PCG32 stream,
+// BVH traversal (fast watertight and reference-order), and the estimator's
+// sampling/evaluation routines (restating src/examples/pt/demo_pt.cpp:416-655 and
+// the src/core functions it calls, with the named extensions GGX, RR, IOR).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "layout.h"
+
+namespace mcrt {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kEpsRay = 1e-4f;   // NUM_EPS_RAY (constants.cpp:13)
+constexpr float kEpsDet = 1e-6f;   // NUM_EPS_DET (constants.cpp:11)
+constexpr float kEpsCos = 1e-6f;   // NUM_EPS_COSINE (constants.cpp:15)
+constexpr int   kSentinel = 0x7fffffff;
+
+// error bits written to the run's error word (never a trap)
+constexpr int kErrStack = 1;
+constexpr int kErrQueue = 2;
+
+// ---------------------------------------------------------------------------
+// float3 helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float3 mk(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator-(float3 a) { return mk(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float  dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b)
+{
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 normalize3(float3 v)
+{
+    float inv = 1.0f / sqrtf(dot3(v, v));
+    return v * inv;
+}
+__device__ __forceinline__ float  maxc(float3 v) { return fmaxf(fmaxf(v.x, v.y), v.z); }
+__device__ __forceinline__ bool   isnan3(float3 v) { return v.x != v.x || v.y != v.y || v.z != v.z; }
+__device__ __forceinline__ float3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
+__device__ __forceinline__ float  comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+__device__ __forceinline__ float  fmax_ref(float a, float b) { return a > b ? a : b; }  // numeric.cpp f_max
+
+// ---------------------------------------------------------------------------
+// PCG32 (O'Neill 2014): state per path slot, stream from the pixel index
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+struct Pcg
+{
+    uint64_t state, inc;
+    __device__ __forceinline__ uint32_t next()
+    {
+        uint64_t old = state;
+        state = old * 6364136223846793005ull + inc;
+        uint32_t xs = static_cast<uint32_t>(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = static_cast<uint32_t>(old >> 59u);
+        return (xs >> rot) | (xs << ((32u - rot) & 31u));
+    }
+    __device__ __forceinline__ float uniform() { return static_cast<float>(next() >> 8) * (1.0f / 16777216.0f); }
+    __device__ __forceinline__ void seed(uint64_t seed, uint32_t pixel, uint32_t sample)
+    {
+        uint64_t initstate = splitmix64(seed ^ (static_cast<uint64_t>(sample) * 0xD1B54A32D192ED03ull));
+        state = 0u;
+        inc = (static_cast<uint64_t>(pixel) << 1u) | 1u;
+        next();
+        state += initstate;
+        next();
+    }
+};
+
+// random numbers drawn per scattering vertex, in this order
+enum Dim
+{
+    D_ENV_LIGHT_0 = 0, D_ENV_LIGHT_1, D_ENV_JITTER_U, D_ENV_JITTER_V, D_ENV_BSDF_0, D_ENV_BSDF_1,
+    D_AREA_BSDF_0, D_AREA_BSDF_1, D_LIGHT_PICK, D_LIGHT_U, D_LIGHT_V, D_CONT_0, D_CONT_1, D_RR,
+    NUM_DIMS
+};
+
+// ---------------------------------------------------------------------------
+// traversal: fast layout (64-B two-child nodes, watertight triangle test)
+// ---------------------------------------------------------------------------
+struct Hit
+{
+    float t, u, v;
+    int   prim;
+};
+
+// Watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2013) with the reference's
+// acceptance rules: |det_MT| >= 1e-6 (triangle.cpp:33-35; det_MT = det * d[kz]) and
+// tmin < t < tmax strictly.  u, v are the barycentrics of b and c as in M-T.
+struct WatertightRay
+{
+    float3 o;
+    int    kx, ky, kz;
+    float  Sx, Sy, Sz;
+    float  det_eps;
+};
+
+__device__ __forceinline__ WatertightRay make_wray(float3 o, float3 d)
+{
+    WatertightRay r;
+    r.o = o;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int   kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int   kx = kz == 2 ? 0 : kz + 1;
+    int   ky = kx == 2 ? 0 : kx + 1;
+    float dz = comp(d, kz);
+    if (dz < 0.f)
+    {
+        int t = kx;
+        kx = ky;
+        ky = t;
+    }
+    r.kx = kx;
+    r.ky = ky;
+    r.kz = kz;
+    r.Sx = comp(d, kx) / dz;
+    r.Sy = comp(d, ky) / dz;
+    r.Sz = 1.0f / dz;
+    r.det_eps = kEpsDet * fabsf(r.Sz);
+    return r;
+}
+
+__device__ __forceinline__ bool watertight(const WatertightRay& r, float3 v0, float3 v1, float3 v2, float tmin,
+                                           float tmax, float& t, float& u, float& v)
+{
+    float3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
+    float  Akz = comp(A, r.kz), Bkz = comp(B, r.kz), Ckz = comp(C, r.kz);
+    float  Ax = comp(A, r.kx) - r.Sx * Akz, Ay = comp(A, r.ky) - r.Sy * Akz;
+    float  Bx = comp(B, r.kx) - r.Sx * Bkz, By = comp(B, r.ky) - r.Sy * Bkz;
+    float  Cx = comp(C, r.kx) - r.Sx * Ckz, Cy = comp(C, r.ky) - r.Sy * Ckz;
+    float  U = Cx * By - Cy * Bx;
+    float  V = Ax * Cy - Ay * Cx;
+    float  W = Bx * Ay - By * Ax;
+    if (U == 0.f || V == 0.f || W == 0.f)
+    {
+        U = static_cast<float>(static_cast<double>(Cx) * By - static_cast<double>(Cy) * Bx);
+        V = static_cast<float>(static_cast<double>(Ax) * Cy - static_cast<double>(Ay) * Cx);
+        W = static_cast<float>(static_cast<double>(Bx) * Ay - static_cast<double>(By) * Ax);
+    }
+    if ((U < 0.f || V < 0.f || W < 0.f) && (U > 0.f || V > 0.f || W > 0.f)) return false;
+    float det = U + V + W;
+    if (!(fabsf(det) >= r.det_eps)) return false;
+    float T = U * (r.Sz * Akz) + V * (r.Sz * Bkz) + W * (r.Sz * Ckz);
+    float inv = 1.0f / det;
+    float tt = T * inv;
+    if (!(tt > tmin && tt < tmax)) return false;
+    t = tt;
+    u = V * inv;
+    v = W * inv;
+    return true;
+}
+
+// Two-child traversal over FastNode with a per-thread stack in shared memory
+// (`stack` points at this thread's column, entries `stride` ints apart).
+template <bool ANY, int STACK>
+__device__ __forceinline__ bool trace_fast(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
+                                           int* stack, int stride, Hit& hit, int* err)
+{
+    const float big = 1e30f;
+    float3      inv = mk(fabsf(d.x) > 1e-30f ? 1.0f / d.x : copysignf(big, d.x),
+                         fabsf(d.y) > 1e-30f ? 1.0f / d.y : copysignf(big, d.y),
+                         fabsf(d.z) > 1e-30f ? 1.0f / d.z : copysignf(big, d.z));
+    float3      ood = o * inv;
+    WatertightRay wr = make_wray(o, d);
+    hit.prim = -1;
+    float best = tmax;
+    int   sp = 0;
+    stack[0] = kSentinel;
+    int cur = 0;
+    while (cur != kSentinel)
+    {
+        // inner nodes
+        while (cur >= 0 && cur != kSentinel)
+        {
+            const float4* np = reinterpret_cast<const float4*>(s.fast_nodes + cur);
+            float4        n0 = __ldg(np + 0);
+            float4        n1 = __ldg(np + 1);
+            float4        n2 = __ldg(np + 2);
+            int4          n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+            float c0lx = n0.x * inv.x - ood.x, c0hx = n0.y * inv.x - ood.x;
+            float c0ly = n0.z * inv.y - ood.y, c0hy = n0.w * inv.y - ood.y;
+            float c0lz = n2.x * inv.z - ood.z, c0hz = n2.y * inv.z - ood.z;
+            float c1lx = n1.x * inv.x - ood.x, c1hx = n1.y * inv.x - ood.x;
+            float c1ly = n1.z * inv.y - ood.y, c1hy = n1.w * inv.y - ood.y;
+            float c1lz = n2.z * inv.z - ood.z, c1hz = n2.w * inv.z - ood.z;
+            float t0n = fmaxf(fmaxf(fminf(c0lx, c0hx), fminf(c0ly, c0hy)), fmaxf(fminf(c0lz, c0hz), tmin));
+            float t0f = fminf(fminf(fmaxf(c0lx, c0hx), fmaxf(c0ly, c0hy)), fminf(fmaxf(c0lz, c0hz), best));
+            float t1n = fmaxf(fmaxf(fminf(c1lx, c1hx), fminf(c1ly, c1hy)), fmaxf(fminf(c1lz, c1hz), tmin));
+            float t1f = fminf(fminf(fmaxf(c1lx, c1hx), fmaxf(c1ly, c1hy)), fminf(fmaxf(c1lz, c1hz), best));
+            // widen the far bound by a few ulp so boxes flat in one axis are not lost
+            bool h0 = t0n <= t0f * 1.0000004f + 1e-30f;
+            bool h1 = t1n <= t1f * 1.0000004f + 1e-30f;
+            if (!h0 && !h1)
+            {
+                cur = stack[sp * stride];
+                --sp;
+            }
+            else
+            {
+                int near = h0 ? n3.x : n3.y;
+                if (h0 && h1)
+                {
+                    int far = n3.y;
+                    if (t1n < t0n)
+                    {
+                        near = n3.y;
+                        far = n3.x;
+                    }
+                    ++sp;
+                    if (sp >= STACK)
+                    {
+                        atomicOr(err, kErrStack);
+                        return hit.prim >= 0;
+                    }
+                    stack[sp * stride] = far;
+                }
+                cur = near;
+            }
+        }
+        // leaves
+        while (cur < 0)
+        {
+            int code = ~cur;
+            int first = code >> 4, count = code & 15;
+            for (int k = 0; k < count; ++k)
+            {
+                const float4* tp = s.fast_tris + 3 * (first + k);
+                float4        a = __ldg(tp + 0);
+                float4        b = __ldg(tp + 1);
+                float4        c = __ldg(tp + 2);
+                float         t, u, v;
+                if (watertight(wr, xyz(a), xyz(b), xyz(c), tmin, best, t, u, v))
+                {
+                    best = t;
+                    hit.t = t;
+                    hit.u = u;
+                    hit.v = v;
+                    hit.prim = __float_as_int(a.w);
+                    if (ANY) return true;
+                }
+            }
+            cur = stack[sp * stride];
+            --sp;
+        }
+    }
+    return hit.prim >= 0;
+}
+
+// ---------------------------------------------------------------------------
+// traversal: reference order and arithmetic (MCRT_TRAVERSE_REF)
+// ---------------------------------------------------------------------------
+struct RefRay
+{
+    float3 o, d, inv;
+    int    sx, sy, sz;  // dir_sign (ray.cpp:44-46)
+    float  tmin, tmax;
+};
+
+__device__ __forceinline__ RefRay make_ref_ray(float3 o, float3 d, float tmin, float tmax)
+{
+    RefRay r;
+    r.o = o;
+    r.d = d;
+    // inv_dir = 0 (not inf) for zero components (ray.cpp:39-42)
+    r.inv = mk(d.x == 0.f ? 0.f : __fdiv_rn(1.0f, d.x), d.y == 0.f ? 0.f : __fdiv_rn(1.0f, d.y),
+               d.z == 0.f ? 0.f : __fdiv_rn(1.0f, d.z));
+    r.sx = d.x < 0.f;
+    r.sy = d.y < 0.f;
+    r.sz = d.z < 0.f;
+    r.tmin = tmin;
+    r.tmax = tmax;
+    return r;
+}
+
+// rayAABBOverlap (aabb.cpp:66-131), every operation rounded as the CPU does it
+__device__ __forceinline__ bool ref_overlap(const RefRay& r, float3 lo, float3 hi)
+{
+    float tmin = __fmul_rn(__fsub_rn(r.sx ? hi.x : lo.x, r.o.x), r.inv.x);
+    float tymin = __fmul_rn(__fsub_rn(r.sy ? hi.y : lo.y, r.o.y), r.inv.y);
+    float tmax = __fmul_rn(__fsub_rn(r.sx ? lo.x : hi.x, r.o.x), r.inv.x);
+    float tymax = __fmul_rn(__fsub_rn(r.sy ? lo.y : hi.y, r.o.y), r.inv.y);
+    if ((tmin > tymax) || (tymin > tmax)) return false;
+    if (tymin > tmin) tmin = tymin;
+    if (tmin > r.tmax) return false;
+    if (tymax < tmax) tmax = tymax;
+    if (tmax < r.tmin) return false;
+    float tzmin = __fmul_rn(__fsub_rn(r.sz ? hi.z : lo.z, r.o.z), r.inv.z);
+    float tzmax = __fmul_rn(__fsub_rn(r.sz ? lo.z : hi.z, r.o.z), r.inv.z);
+    if ((tmin > tzmax) || (tzmin > tmax)) return false;
+    if (tzmin > tmin) tmin = tzmin;
+    if (tmin > r.tmax) return false;
+    if (tzmax < tmax) tmax = tzmax;
+    if (tmax < r.tmin) return false;
+    return true;
+}
+
+__device__ __forceinline__ float3 sub_rn(float3 a, float3 b)
+{
+    return mk(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+__device__ __forceinline__ float3 cross_rn(float3 a, float3 b)
+{
+    return mk(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+              __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float dot_rn(float3 a, float3 b)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+
+// rayTriangleIntersect, MOLLER_TRUMBORE branch (triangle.cpp:13-51)
+__device__ __forceinline__ bool ref_mt(float3 orig, float3 dir, float3 v0, float3 v1, float3 v2, float& t, float& u,
+                                       float& v)
+{
+    float3 v0v1 = sub_rn(v1, v0);
+    float3 v0v2 = sub_rn(v2, v0);
+    float3 pvec = cross_rn(dir, v0v2);
+    float  det = dot_rn(v0v1, pvec);
+    if (fabsf(det) < kEpsDet) return false;
+    float  invDet = __fdiv_rn(1.0f, det);
+    float3 tvec = sub_rn(orig, v0);
+    u = __fmul_rn(dot_rn(tvec, pvec), invDet);
+    if (u < 0.f || u > 1.f) return false;
+    float3 qvec = cross_rn(tvec, v0v1);
+    v = __fmul_rn(dot_rn(dir, qvec), invDet);
+    if (v < 0.f || __fadd_rn(u, v) > 1.f) return false;
+    t = __fmul_rn(dot_rn(v0v2, qvec), invDet);
+    return true;
+}
+
+// Iterative form of SplitBVHBranchNode/LeafNode::intersect (splitbvh.cpp:5-145):
+// a node's own box is tested when it is visited (against the current tmax), leaf
+// references are culled by their clipped bounds, children are visited left-first
+// iff dir[split_axis] > 0, and ties keep the first hit found.
+template <bool ANY, int STACK>
+__device__ __forceinline__ bool trace_ref(const SceneView& s, float3 o, float3 d, float tmin, float tmax, int* stack,
+                                          int stride, Hit& hit, int* err)
+{
+    RefRay r = make_ref_ray(o, d, tmin, tmax);
+    hit.prim = -1;
+    int sp = 0;
+    stack[0] = 0;
+    sp = 1;
+    while (sp > 0)
+    {
+        --sp;
+        int     n = stack[sp * stride];
+        RefNode rn;
+        rn.lo = __ldg(&s.ref_nodes[n].lo);
+        rn.hi = __ldg(&s.ref_nodes[n].hi);
+        if (!ref_overlap(r, xyz(rn.lo), xyz(rn.hi))) continue;
+        int a = __float_as_int(rn.lo.w), b = __float_as_int(rn.hi.w);
+        if (a < 0)
+        {
+            int first = ~a;
+            for (int k = 0; k < b; ++k)
+            {
+                float4 plo = __ldg(&s.ref_prims[first + k].lo);
+                float4 phi = __ldg(&s.ref_prims[first + k].hi);
+                if (!ref_overlap(r, xyz(plo), xyz(phi))) continue;
+                int           prim = __float_as_int(plo.w);
+                const float4* pv = s.prim_verts + 3 * prim;
+                float         t, u, v;
+                if (ref_mt(r.o, r.d, xyz(__ldg(pv)), xyz(__ldg(pv + 1)), xyz(__ldg(pv + 2)), t, u, v) && t > r.tmin &&
+                    t < r.tmax)
+                {
+                    r.tmax = t;
+                    hit.t = t;
+                    hit.u = u;
+                    hit.v = v;
+                    hit.prim = prim;
+                    if (ANY) return true;
+                }
+            }
+        }
+        else
+        {
+            int  left = a, right = b >> 2, axis = b & 3;
+            bool left_first = comp(r.d, axis) > 0.0f;
+            if (sp + 2 > STACK)
+            {
+                atomicOr(err, kErrStack);
+                return hit.prim >= 0;
+            }
+            stack[sp * stride] = left_first ? right : left;
+            ++sp;
+            stack[sp * stride] = left_first ? left : right;
+            ++sp;
+        }
+    }
+    return hit.prim >= 0;
+}
+
+template <bool ANY, int STACK>
+__device__ __forceinline__ bool trace_ray(const SceneView& s, int mode, float3 o, float3 d, float tmin, float tmax,
+                                          int* stack, int stride, Hit& hit, int* err)
+{
+    if (mode == 1) return trace_ref<ANY, STACK>(s, o, d, tmin, tmax, stack, stride, hit, err);
+    bool found = trace_fast<ANY, STACK>(s, o, d, tmin, tmax, stack, stride, hit, err);
+    if (!ANY && found)
+    {
+        // The watertight test decides which triangle is closest; the reported t, u, v
+        // of that one triangle are then recomputed with the reference's Moller-Trumbore
+        // arithmetic (each formula lands ~3 ulp from the exact t, on either side).
+        const float4* pv = s.prim_verts + 3 * hit.prim;
+        float         t, u, v;
+        if (ref_mt(o, d, xyz(__ldg(pv)), xyz(__ldg(pv + 1)), xyz(__ldg(pv + 2)), t, u, v) && t > tmin)
+        {
+            hit.t = t;
+            hit.u = u;
+            hit.v = v;
+        }
+    }
+    return found;
+}
+
+// ---------------------------------------------------------------------------
+// shading data
+// ---------------------------------------------------------------------------
+// TriangleObject::normal(u, v) (triangle.cpp:90-93); material id in .w of na
+__device__ __forceinline__ float3 shading_normal(const SceneView& s, int prim, float u, float v, int& mat)
+{
+    const float4* p = s.prim_shade + 3 * prim;
+    float4        na = __ldg(p), nb = __ldg(p + 1), nc = __ldg(p + 2);
+    mat = __float_as_int(na.w);
+    float w = 1.0f - u - v;
+    return normalize3(xyz(na) * w + xyz(nb) * u + xyz(nc) * v);
+}
+
+struct Mat
+{
+    int    type;
+    float3 color;
+    float  roughness, ior;
+    int    albedo_param, emission_param;
+};
+
+__device__ __forceinline__ Mat load_mat(const SceneView& s, int m)
+{
+    MaterialGPU g = s.materials[m];
+    Mat         r;
+    r.type = g.type;
+    r.color = mk(g.r, g.g, g.b);
+    r.roughness = g.roughness;
+    r.ior = g.ior;
+    r.albedo_param = g.albedo_param;
+    r.emission_param = g.emission_param;
+    return r;
+}
+
+constexpr int MAT_LGHT = 0, MAT_DIFF = 1, MAT_SPEC = 2, MAT_REFR = 3, MAT_GLSY = 4, MAT_GGX = 8;
+__device__ __forceinline__ bool does_nee(int type) { return type == MAT_DIFF || type == MAT_GGX; }
+
+// OrthonormalFrame::setFromNormal (geometry.cpp:74-105; Duff et al. 2017)
+struct Frame
+{
+    float3 x, y, z;
+    __device__ __forceinline__ explicit Frame(float3 n)
+    {
+        float       sign = copysignf(1.0f, n.z);
+        const float a = -1.0f / (sign + n.z);
+        const float b = n.x * n.y * a;
+        x = mk(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+        y = mk(b, sign + n.y * n.y * a, -n.y);
+        z = n;
+    }
+    __device__ __forceinline__ float3 to_world(float3 c) const { return x * c.x + y * c.y + z * c.z; }
+    __device__ __forceinline__ float3 to_local(float3 v) const { return mk(dot3(v, x), dot3(v, y), dot3(v, z)); }
+};
+
+__device__ __forceinline__ float3 reflect_world(float3 wi, float3 n) { return n * (2.0f * dot3(n, wi)) - wi; }
+
+// fresnelReflectance (geometry.cpp:14-43)
+__device__ __forceinline__ float fresnel(float cos_i, float ior)
+{
+    if (ior < 0.f) return 1.f;
+    float eta;
+    if (cos_i < 0.f)
+    {
+        cos_i = -cos_i;
+        eta = ior;
+    }
+    else
+    {
+        eta = 1.0f / ior;
+    }
+    float sin2t = fminf(1.0f, (eta * eta) * (1.0f - cos_i * cos_i));
+    float cos_t = sqrtf(1.0f - sin2t);
+    float t1 = eta * cos_t;
+    float rs = (cos_i - t1) / (cos_i + t1);
+    float t2 = eta * cos_i;
+    float rp = (t2 - cos_t) / (t2 + cos_t);
+    return (rs * rs + rp * rp) * 0.5f;
+}
+
+// GGX (Walter et al. 2007), local frame z = normal
+__device__ __forceinline__ float ggx_D(float3 h, float a)
+{
+    float a2 = a * a;
+    float d = h.z * h.z * (a2 - 1.0f) + 1.0f;
+    return a2 / (kPi * d * d);
+}
+__device__ __forceinline__ float ggx_G1(float3 v, float a)
+{
+    float c2 = v.z * v.z;
+    if (c2 <= 0.f) return 0.f;
+    float t2 = (1.0f - c2) / c2;
+    return 2.0f / (1.0f + sqrtf(1.0f + a * a * t2));
+}
+__device__ __forceinline__ float3 schlick(float3 f0, float c)
+{
+    float m = 1.0f - c;
+    float m5 = m * m * m * m * m;
+    return f0 + (mk(1.f, 1.f, 1.f) - f0) * m5;
+}
+
+struct BsdfSample
+{
+    float3 wo;
+    float3 weight;
+    float  pdf;
+};
+
+// Material::sample (bsdf.cpp Lambert :51-87, Specular :134-162, Glossy :209-262,
+// Refractive :319-418) plus the GGX conductor (Heitz 2018 visible normals)
+__device__ __forceinline__ BsdfSample bsdf_sample(const Mat& m, float3 wi, float3 nl, float r1, float r2)
+{
+    BsdfSample s;
+    s.pdf = 0.f;
+    if (m.type == MAT_SPEC)
+    {
+        s.wo = reflect_world(wi, nl);
+        s.weight = m.color;
+        s.pdf = 1.f;
+    }
+    else if (m.type == MAT_REFR)
+    {
+        bool   outside = dot3(wi, nl) > 0.f;
+        float3 n = outside ? nl : -nl;
+        float3 refl = normalize3(reflect_world(wi, n));
+        float  nc = 1.f, nt = m.ior;
+        float  nnt = outside ? nc / nt : nt / nc;
+        float  ddn = dot3(-wi, n);
+        float  cos2t = 1.f - nnt * nnt * (1.f - ddn * ddn);
+        if (cos2t < 0.f)
+        {
+            s.weight = m.color;
+            s.pdf = 1.f;
+            s.wo = refl;
+        }
+        else
+        {
+            float3 tdir = normalize3(-wi * nnt - n * (ddn * nnt + sqrtf(cos2t)));
+            float  Re = fresnel(dot3(wi, nl), nt / nc);
+            float  Tr = 1.f - Re;
+            float  P = Re;
+            if (r1 < P)
+            {
+                s.weight = m.color * (Re / P);
+                s.pdf = P;
+                s.wo = refl;
+            }
+            else
+            {
+                s.weight = m.color * (Tr / (1.f - P));
+                s.pdf = 1.f - P;
+                s.wo = tdir;
+            }
+        }
+    }
+    else if (m.type == MAT_GLSY)
+    {
+        const float g = 25.f;
+        float       x = r1 * (2.f * kPi);
+        float       r2p = powf(r2, 1.0f / (g + 1.0f));
+        float       st = sqrtf(1.0f - r2p * r2p);
+        float3      c = mk(sinf(x) * st, cosf(x) * st, r2p);
+        float3      refl = reflect_world(wi, nl);
+        Frame       onb(refl);
+        float3      wo = onb.to_world(c);
+        if (dot3(wo, nl) < 0.f) wo = mk(0.f, 0.f, 0.f);
+        float c_o = fmax_ref(dot3(wo, nl), kEpsCos);
+        s.pdf = (g + 1.f) / (2.f * kPi) * powf(fmax_ref(dot3(refl, wo), kEpsCos), g);
+        float w = (g + 2.f) / (g + 1.f) * c_o / fmax_ref(fabsf(dot3(wi, nl)), fabsf(dot3(wo, nl)));
+        if (w != w) w = 0.f;
+        s.weight = m.color * w;
+        s.wo = wo;
+    }
+    else if (m.type == MAT_GGX)
+    {
+        float3 n = dot3(wi, nl) < 0.f ? -nl : nl;
+        Frame  fr(n);
+        float3 wl = fr.to_local(wi);
+        float  a = m.roughness;
+        s.wo = n;
+        s.weight = mk(0.f, 0.f, 0.f);
+        if (wl.z > 0.f)
+        {
+            float3 vh = normalize3(mk(a * wl.x, a * wl.y, wl.z));
+            float  lensq = vh.x * vh.x + vh.y * vh.y;
+            float3 t1 = lensq > 0.f ? mk(-vh.y, vh.x, 0.f) * rsqrtf(lensq) : mk(1.f, 0.f, 0.f);
+            float3 t2 = cross3(vh, t1);
+            float  r = sqrtf(r1);
+            float  phi = 2.f * kPi * r2;
+            float  p1 = r * cosf(phi);
+            float  p2 = r * sinf(phi);
+            float  sh = 0.5f * (1.f + vh.z);
+            p2 = (1.f - sh) * sqrtf(fmaxf(0.f, 1.f - p1 * p1)) + sh * p2;
+            float3 nh = t1 * p1 + t2 * p2 + vh * sqrtf(fmaxf(0.f, 1.f - p1 * p1 - p2 * p2));
+            float3 h = normalize3(mk(a * nh.x, a * nh.y, fmaxf(0.f, nh.z)));
+            float  wih = dot3(wl, h);
+            float3 ol = h * (2.f * wih) - wl;
+            s.wo = fr.to_world(ol);
+            if (ol.z > 0.f && wih > 0.f)
+            {
+                s.pdf = ggx_G1(wl, a) * ggx_D(h, a) / (4.f * wl.z);
+                s.weight = schlick(m.color, wih) * ggx_G1(ol, a);
+            }
+        }
+    }
+    else  // DIFF (and any other type, as Material's default)
+    {
+        float  x = r1 * (2.f * kPi);
+        float  r2s = sqrtf(r2);
+        float3 c = mk(cosf(x) * r2s, sinf(x) * r2s, sqrtf(1.f - r2));
+        Frame  onb(nl);
+        float3 wo = onb.to_world(c);
+        float  c_o = fmax_ref(dot3(wo, nl), kEpsCos);
+        s.pdf = c_o / kPi;
+        s.weight = m.color;
+        s.wo = wo;
+    }
+    return s;
+}
+
+// Material::pdfW
+__device__ __forceinline__ float bsdf_pdf(const Mat& m, float3 wi, float3 nl, float3 wo)
+{
+    if (m.type == MAT_DIFF) return fmax_ref(dot3(wo, nl), kEpsCos) / kPi;
+    if (m.type == MAT_GLSY)
+    {
+        float3 refl = reflect_world(wi, nl);
+        return 26.f / (2.f * kPi) * powf(fmax_ref(dot3(refl, wo), kEpsCos), 25.f);
+    }
+    if (m.type == MAT_GGX)
+    {
+        float3 n = dot3(wi, nl) < 0.f ? -nl : nl;
+        Frame  fr(n);
+        float3 wl = fr.to_local(wi), ol = fr.to_local(wo);
+        if (wl.z <= 0.f || ol.z <= 0.f) return 0.f;
+        float3 h = normalize3(wl + ol);
+        return ggx_G1(wl, m.roughness) * ggx_D(h, m.roughness) / (4.f * wl.z);
+    }
+    return 0.f;
+}
+
+// Material::evaluate: the BSDF value without the cosine
+__device__ __forceinline__ float3 bsdf_eval(const Mat& m, float3 wi, float3 nl, float3 wo)
+{
+    if (m.type == MAT_DIFF) return m.color * (1.0f / kPi);
+    if (m.type == MAT_GLSY)
+    {
+        float3 refl = reflect_world(wi, nl);
+        float  v = 27.f / (2.f * kPi) * powf(fmax_ref(dot3(refl, wo), kEpsCos), 25.f) /
+                  fmax_ref(fabsf(dot3(wi, nl)), fabsf(dot3(wo, nl)));
+        return m.color * v;
+    }
+    if (m.type == MAT_GGX)
+    {
+        float3 n = dot3(wi, nl) < 0.f ? -nl : nl;
+        Frame  fr(n);
+        float3 wl = fr.to_local(wi), ol = fr.to_local(wo);
+        if (wl.z <= 0.f || ol.z <= 0.f) return mk(0.f, 0.f, 0.f);
+        float3 h = normalize3(wl + ol);
+        float  a = m.roughness;
+        float  v = ggx_D(h, a) * ggx_G1(wl, a) * ggx_G1(ol, a) / (4.f * wl.z * ol.z);
+        return schlick(m.color, dot3(wl, h)) * v;
+    }
+    return mk(0.f, 0.f, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// environment map (envmap.cpp:44-53, :333-506)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int clampi(int x, int a, int b) { return x < a ? a : (x > b ? b : x); }
+
+__device__ __forceinline__ int lower_bound_cdf(const float* cdf, int n, float r)  // DiscreteSampler::sample
+{
+    int begin = 0, end = n - 1;
+    while (end > begin)
+    {
+        int mid = begin + (end - begin) / 2;
+        if (__ldg(cdf + mid) >= r)
+            end = mid;
+        else
+            begin = mid + 1;
+    }
+    return begin;
+}
+
+__device__ __forceinline__ float env_pdf_at(const SceneView& s, int ui, int vi)
+{
+    float lum = __ldg(&s.env_rgb[ui + vi * s.env_w].w);
+    return s.env_norm * lum * static_cast<float>(s.env_w) * static_cast<float>(s.env_h) / (2.f * kPi * kPi);
+}
+
+__device__ __forceinline__ void env_texel(const SceneView& s, float3 d, int& ui, int& vi)
+{
+    float phi = acosf(d.y);
+    float theta = atanf(d.z / d.x) + kPi * 0.5f;
+    if (d.x < 0.f) theta += kPi;
+    ui = clampi(static_cast<int>(theta / (kPi * 2.f) * static_cast<float>(s.env_w)), 0, s.env_w - 1);
+    vi = clampi(static_cast<int>(phi / kPi * static_cast<float>(s.env_h)), 0, s.env_h - 1);
+}
+
+__device__ __forceinline__ float env_pdf(const SceneView& s, float3 d)
+{
+    int ui, vi;
+    env_texel(s, d, ui, vi);
+    return env_pdf_at(s, ui, vi);
+}
+
+__device__ __forceinline__ float3 env_radiance(const SceneView& s, float3 d)
+{
+    int ui, vi;
+    env_texel(s, d, ui, vi);
+    return xyz(__ldg(&s.env_rgb[ui + vi * s.env_w]));
+}
+
+// EnvmapLoader::sample with the two texel-jitter numbers explicit
+__device__ __forceinline__ void env_sample(const SceneView& s, float r1, float r2, float j1, float j2, float3& dir,
+                                           float3& rad, float& pdf)
+{
+    int   W = s.env_w, H = s.env_h;
+    int   ui0 = lower_bound_cdf(s.env_marginal, W, r1);
+    int   vi0 = lower_bound_cdf(s.env_cond + static_cast<size_t>(ui0) * H, H, r2);
+    float u = (static_cast<float>(ui0) + j1) / static_cast<float>(W);
+    float v = (static_cast<float>(vi0) + j2) / static_cast<float>(H);
+    int   ui = clampi(static_cast<int>(u * static_cast<float>(W)), 0, W - 1);
+    int   vi = clampi(static_cast<int>(v * static_cast<float>(H)), 0, H - 1);
+    float phi = v * kPi;
+    float theta = u * 2.f * kPi;
+    float sp = sinf(phi);
+    dir = mk(sp * sinf(theta), cosf(phi), sp * -cosf(theta));
+    pdf = env_pdf_at(s, ui, vi);
+    rad = xyz(__ldg(&s.env_rgb[ui + vi * W]));
+}
+
+// Camera::makeRay (camera.cpp:37-43)
+__device__ __forceinline__ void camera_ray(const CameraGPU& c, float mx, float my, float3& o, float3& d)
+{
+    float3 su = mk(c.fxx, c.fxy, c.fxz) * ((mx - 0.5f) * c.film_w);
+    float3 sv = mk(c.fyx, c.fyy, c.fyz) * ((my - 0.5f) * c.film_h);
+    float3 sw = mk(c.wx, c.wy, c.wz) * c.dist;
+    o = mk(c.ox, c.oy, c.oz);
+    d = normalize3(su + sv + sw);
+}
+
+// tent-filtered sample position (demo_pt.cpp:689-697)
+__device__ __forceinline__ float tent(float r) { return r < 1.f ? sqrtf(r) - 1.f : 1.f - sqrtf(2.f - r); }
+
+}  // namespace mcrt

@@ -1,0 +1,55 @@
+// Host-side scene preparation: BVH construction, flattening into the device layouts,
+// emitter and environment-map sampling tables.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "layout.h"
+
+namespace mcrt {
+
+// A binary BVH in the form of the C ABI's mcrt_bvh_tree (see mcrt_gb300.h).
+struct BinaryTree
+{
+    std::vector<float>   node_box;   // 6 per node
+    std::vector<int32_t> node_info;  // 6 per node: is_leaf, left, right, axis, ref_begin, ref_count
+    std::vector<int32_t> ref_prim;
+    std::vector<float>   ref_box;    // 6 per ref
+    int                  root = 0;
+};
+
+// Binned-SAH object-split builder (own design; leaf <= leaf_size references).
+// Multithreaded over subtrees.  Leaves reference contiguous runs of ref_prim.
+void build_sah_tree(const float* vertices, int64_t num_tris, int leaf_size, BinaryTree& out);
+
+struct FlatBVH
+{
+    std::vector<FastNode> fast_nodes;
+    std::vector<float4>   fast_tris;  // 3 per reference
+    std::vector<RefNode>  ref_nodes;
+    std::vector<RefPrim>  ref_prims;
+    int                   max_depth = 0;
+};
+
+// Validates the tree and emits both device layouts in depth-first order.
+// Returns an empty string on success, else an error message.
+std::string flatten_tree(const BinaryTree& tree, const float* vertices, int64_t num_tris, FlatBVH& out);
+
+struct HostScene
+{
+    FlatBVH                  bvh;
+    std::vector<float4>      prim_verts;  // 3 per prim
+    std::vector<float4>      prim_shade;  // 3 per prim
+    std::vector<int32_t>     light_of;
+    std::vector<LightGPU>    lights;
+    float                    light_area = 0.f;
+    std::vector<MaterialGPU> materials;
+    int                      env_w = 0, env_h = 0;
+    std::vector<float4>      env_rgb;
+    std::vector<float>       env_marginal;
+    std::vector<float>       env_cond;
+    float                    env_norm = 0.f;
+};
+
+}  // namespace mcrt

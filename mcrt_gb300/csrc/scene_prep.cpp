@@ -1,0 +1,209 @@
+// Host-side scene assembly: BVH (own builder or a given tree), per-primitive
+// shading data, the emitter table and the environment-map sampling tables.
+// Compiled with -ffp-contract=off so the float tables follow the reference's
+// operation order exactly:
+//   face normal  TriangleObject ctor   triangle.cpp:71   normalize(cross(a - c, b - c))
+//   area         TriangleObject::area  triangle.cpp:129-132
+//   emitter CDF  Scene::finalize + DiscreteSampler::update  scene.cpp:151-178, sample.cpp:96-112
+//   envmap CDFs  EnvmapLoader::buildCdf  envmap.cpp:208-331 (luminance numeric.cpp:62-66)
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mcrt_gb300.h"
+#include "host.h"
+
+namespace mcrt {
+namespace {
+
+struct V
+{
+    float x, y, z;
+};
+inline V      ld(const float* p) { return V{p[0], p[1], p[2]}; }
+inline V      sub(V a, V b) { return V{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V      cross(V a, V b)
+{
+    return V{(a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x)};
+}
+inline float  len(V v) { return std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+inline V      normalize(V v)
+{
+    float inv = 1.0f / len(v);
+    return V{v.x * inv, v.y * inv, v.z * inv};
+}
+inline float4 f4(V v, float w) { return float4{v.x, v.y, v.z, w}; }
+inline float  ibits(int32_t i)
+{
+    float f;
+    std::memcpy(&f, &i, 4);
+    return f;
+}
+
+// DiscreteSampler::update: pdf = data * (1 / sum), cdf = running float sum
+void discrete(const std::vector<float>& data, std::vector<float>& pdf, std::vector<float>& cdf)
+{
+    pdf = data;
+    cdf.resize(data.size());
+    float norm = 0.0f;
+    for (float d : pdf) norm += d;
+    float inv = 1.0f / norm;
+    for (auto& p : pdf) p = p * inv;
+    float sum = 0.0f;
+    for (size_t n = 0; n < pdf.size(); ++n)
+    {
+        sum += pdf[n];
+        cdf[n] = sum;
+    }
+}
+
+}  // namespace
+
+std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs)
+{
+    const int64_t n = d.num_triangles;
+    if (n <= 0 || !d.vertices || !d.material_ids || d.num_materials <= 0 || !d.materials)
+        return "scene needs triangles, material ids and materials";
+    if (n >= (int64_t(1) << 27)) return "more than 2^27 triangles";
+    for (int64_t i = 0; i < n; ++i)
+        if (d.material_ids[i] < 0 || d.material_ids[i] >= d.num_materials) return "material id out of range";
+    hs.materials.resize(d.num_materials);
+    for (int m = 0; m < d.num_materials; ++m)
+    {
+        const mcrt_material& s = d.materials[m];
+        if (s.type != MCRT_MAT_LGHT && s.type != MCRT_MAT_DIFF && s.type != MCRT_MAT_SPEC && s.type != MCRT_MAT_REFR &&
+            s.type != MCRT_MAT_GLSY && s.type != MCRT_MAT_GGX)
+            return "unknown material type";
+        MaterialGPU& g = hs.materials[m];
+        g.type = s.type;
+        g.r = s.color[0];
+        g.g = s.color[1];
+        g.b = s.color[2];
+        g.roughness = s.roughness;
+        g.ior = s.ior;
+        g.albedo_param = s.albedo_param;
+        g.emission_param = s.emission_param;
+    }
+
+    // BVH
+    BinaryTree tree;
+    if (d.builder == MCRT_BUILD_EXTERNAL)
+    {
+        const mcrt_bvh_tree* t = d.external_tree;
+        if (!t || t->num_nodes <= 0 || t->num_refs < 0 || !t->node_box || !t->node_info || !t->ref_prim || !t->ref_box)
+            return "external_tree missing or empty";
+        tree.node_box.assign(t->node_box, t->node_box + 6 * static_cast<size_t>(t->num_nodes));
+        tree.node_info.assign(t->node_info, t->node_info + 6 * static_cast<size_t>(t->num_nodes));
+        tree.ref_prim.assign(t->ref_prim, t->ref_prim + t->num_refs);
+        tree.ref_box.assign(t->ref_box, t->ref_box + 6 * static_cast<size_t>(t->num_refs));
+        tree.root = 0;
+    }
+    else if (d.builder == MCRT_BUILD_SAH)
+    {
+        int leaf = d.leaf_size > 0 ? d.leaf_size : 4;
+        if (leaf > 15) return "leaf_size must be <= 15";
+        build_sah_tree(d.vertices, n, leaf, tree);
+    }
+    else
+    {
+        return "unknown builder";
+    }
+    std::string err = flatten_tree(tree, d.vertices, n, hs.bvh);
+    if (!err.empty()) return err;
+
+    // per-primitive vertices and shading normals
+    hs.prim_verts.resize(3 * n);
+    hs.prim_shade.resize(3 * n);
+    hs.light_of.assign(n, -1);
+    std::vector<float> areas;
+    for (int64_t i = 0; i < n; ++i)
+    {
+        const float* p = d.vertices + 9 * i;
+        V            a = ld(p), b = ld(p + 3), c = ld(p + 6);
+        hs.prim_verts[3 * i + 0] = f4(a, 0.f);
+        hs.prim_verts[3 * i + 1] = f4(b, 0.f);
+        hs.prim_verts[3 * i + 2] = f4(c, 0.f);
+        V na, nb, nc;
+        if (d.normals)
+        {
+            na = ld(d.normals + 9 * i);
+            nb = ld(d.normals + 9 * i + 3);
+            nc = ld(d.normals + 9 * i + 6);
+        }
+        else
+        {
+            na = nb = nc = normalize(cross(sub(a, c), sub(b, c)));
+        }
+        hs.prim_shade[3 * i + 0] = f4(na, ibits(d.material_ids[i]));
+        hs.prim_shade[3 * i + 1] = f4(nb, 0.f);
+        hs.prim_shade[3 * i + 2] = f4(nc, 0.f);
+        if (d.materials[d.material_ids[i]].type == MCRT_MAT_LGHT)
+        {
+            hs.light_of[i] = static_cast<int32_t>(hs.lights.size());
+            LightGPU l;
+            l.prim = static_cast<int>(i);
+            l.area = len(cross(sub(b, a), sub(c, a))) * 0.5f;
+            l.pdf = l.cdf = 0.f;
+            hs.lights.push_back(l);
+            areas.push_back(l.area);
+        }
+    }
+    if (!areas.empty())
+    {
+        std::vector<float> pdf, cdf;
+        discrete(areas, pdf, cdf);
+        float la = 0.0f;
+        for (size_t k = 0; k < areas.size(); ++k)
+        {
+            hs.lights[k].pdf = pdf[k];
+            hs.lights[k].cdf = cdf[k];
+            la += areas[k];
+        }
+        hs.light_area = la;
+    }
+
+    // environment map
+    if (d.env_rgb && d.env_width > 0 && d.env_height > 0)
+    {
+        int M = d.env_height, N = d.env_width;
+        hs.env_w = N;
+        hs.env_h = M;
+        std::vector<float> lum(static_cast<size_t>(M) * N);
+        hs.env_rgb.resize(lum.size());
+        for (size_t k = 0; k < lum.size(); ++k)
+        {
+            const float* c = d.env_rgb + 3 * k;
+            lum[k] = static_cast<float>(0.299 * c[0] + 0.587 * c[1] + 0.114 * c[2]);
+            hs.env_rgb[k] = float4{c[0], c[1], c[2], lum[k]};
+        }
+        const float pi = 3.14159265358979323846f;
+        for (int m = 0; m < M; ++m)
+        {
+            float phi = pi * (m + 0.5f) / M;
+            for (int k = 0; k < N; ++k) lum[k + static_cast<size_t>(m) * N] *= std::sin(phi);
+        }
+        float acc = 0.0f;
+        for (float v : lum) acc += v;
+        hs.env_norm = 1.0f / acc;
+        std::vector<float> colsum(N), col(M), pdf, cdf;
+        hs.env_cond.resize(static_cast<size_t>(M) * N);
+        for (int k = 0; k < N; ++k)
+        {
+            float s = 0.0f;
+            for (int m = 0; m < M; ++m)
+            {
+                col[m] = lum[k + static_cast<size_t>(m) * N];
+                s += col[m];
+            }
+            colsum[k] = s;
+            discrete(col, pdf, cdf);
+            std::memcpy(&hs.env_cond[static_cast<size_t>(k) * M], cdf.data(), sizeof(float) * M);
+        }
+        discrete(colsum, pdf, cdf);
+        hs.env_marginal = cdf;
+    }
+    return std::string();
+}
+
+}  // namespace mcrt

@@ -1,0 +1,85 @@
+"""The C-ABI library: builds, loads, exports every entry point include/mcrt_gb300.h
+declares, and rejects bad arguments with a status code and a message (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from conftest import ROOT
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "mcrt_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mcrt_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(native):
+    names = _declared()
+    assert "mcrt_render" in names and "mcrt_trace_closest" in names
+    for n in names:
+        assert hasattr(native, n), f"{n} declared but not exported"
+    assert native.mcrt_get_abi_version() == 1
+
+
+def test_null_arguments_fail_cleanly(native):
+    from mcrt_gb300 import _native as N
+    out = ctypes.c_void_p()
+    rc = native.mcrt_scene_create(None, ctypes.byref(out))
+    assert rc == -1 and out.value is None
+    assert b"null" in native.mcrt_last_error()
+    cam = N.Camera()
+    p = N.RenderParams()
+    rc = native.mcrt_render(None, ctypes.byref(cam), ctypes.byref(p), None, None, None)
+    assert rc == -1
+    rc = native.mcrt_trace_closest(None, None, 0, None, 0, 0, None)
+    assert rc == -1
+    assert native.mcrt_scene_destroy(None) == 0
+
+
+def test_scene_desc_validation_before_any_device_work(native):
+    """Malformed descriptions are rejected on the host (no CUDA call is reached)."""
+    from mcrt_gb300 import _native as N
+    v = np.zeros((1, 9), np.float32)
+    mid = np.array([3], np.int32)  # out of range
+    mats = (N.Material * 1)()
+    d = N.SceneDesc()
+    d.num_triangles = 1
+    d.vertices = v.ctypes.data
+    d.material_ids = mid.ctypes.data
+    d.num_materials = 1
+    d.materials = mats
+    out = ctypes.c_void_p()
+    assert native.mcrt_scene_create(ctypes.byref(d), ctypes.byref(out)) == -1
+    assert b"material id" in native.mcrt_last_error()
+    mid[0] = 0
+    mats[0].type = 77
+    assert native.mcrt_scene_create(ctypes.byref(d), ctypes.byref(out)) == -1
+    assert b"material type" in native.mcrt_last_error()
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """ctypes mirrors of the C structs have the sizes and field offsets the C compiler
+    gives the header's structs."""
+    import subprocess
+    from mcrt_gb300 import _native as N
+    pairs = {"mcrt_material": N.Material, "mcrt_bvh_tree": N.BvhTree, "mcrt_scene_desc": N.SceneDesc,
+             "mcrt_ray": N.Ray, "mcrt_hit": N.Hit, "mcrt_camera": N.Camera, "mcrt_render_params": N.RenderParams,
+             "mcrt_render_stats": N.RenderStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "mcrt_gb300.h"', "int main(void) {"]
+    for cname, py in pairs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    c = tmp_path / "layout.c"
+    c.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", f"-I{os.path.join(ROOT, 'include')}", str(c), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True)
+               .stdout.splitlines())
+    for cname, py in pairs.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, f"{cname}.{fname}"
