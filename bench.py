@@ -1,0 +1,304 @@
+#!/usr/bin/env python
+"""Benchmark: the path tracer on the large plain configuration.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload cfg1|cfg0]
+
+One step = one complete render of the workload (default cfg1: displaced level-8
+icosphere, 1,310,722 triangles, procedural 1024x512 environment map with a sun,
+Lambert/GGX/dielectric patches, 1024x1024 pixels, 64 spp, depth 16) with the scene
+resident on the GPU.  Metric: Mrays/s (every extension and next-event ray traced),
+with samples/s beside it.  Under torchrun (N > 1) every rank renders its own replica
+(the path tracer does not shard across GPUs here): weak scaling, value = rays of all
+ranks / max time.
+
+--impl reference times the reference's CPU path on this machine's cores instead (the
+reference's own compiled code when it is available and the workload is small enough
+to build its BVH quickly, otherwise the oracle's float port of the same estimator).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s & samples/s per GB300 at fixed FP64-oracle RMSE; adjoint/forward ratio"
+UNIT = "Mrays/s"
+
+
+def workload(name: str):
+    from mcrt_gb300 import scenes
+    if name == "cfg0":
+        desc = scenes.cfg0_scene()
+        cam = scenes.cfg0_camera(256, 256)
+        p = dict(spp=16, max_depth=8, rr_depth=3)
+        text = "cfg0: Cornell box + level-4 icosphere (5,132 T), 256x256, 16 spp, depth 8, RR from 3"
+    else:
+        desc = scenes.cfg1_scene()
+        cam = scenes.cfg1_camera(1024, 1024)
+        p = dict(spp=64, max_depth=16, rr_depth=-1)
+        text = ("cfg1: displaced level-8 icosphere + ground (1,310,722 T), 1024x512 envmap with 0.5 deg sun, "
+                "40/30/30 Lambert/GGX/dielectric patches, 1024x1024, 64 spp, depth 16")
+    return desc, cam, p, text
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_port_sample(desc, cam, p, rows, seed=7):
+    """The oracle's float port of the estimator on all host cores, over a band of rows."""
+    from oracle.oracle import OracleScene
+    t0 = time.time()
+    osc = OracleScene(desc, 32)
+    build_s = time.time() - t0
+    r0, r1 = rows
+    t0 = time.time()
+    out = osc.render(cam.as_array(), cam.width, cam.height, p["spp"], p["max_depth"], p["rr_depth"], seed=seed,
+                     rows=(r0, r1), threads=os.cpu_count())
+    dt = time.time() - t0
+    return out["rays"], (r1 - r0) * cam.width * p["spp"], dt, build_s
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    desc, cam, p, text = workload(args.workload)
+    cores = os.cpu_count() or 1
+    # rows per step sized for a few seconds of CPU work
+    rows_per_step = {"cfg0": 64, "cfg1": 8}.get(args.workload, 8)
+    kind = "port"
+    times, rays_total = [], 0
+    for step in range(args.warmup + args.steps):
+        r0 = (step * rows_per_step) % cam.height
+        rays, paths, dt, _ = cpu_port_sample(desc, cam, p, (r0, min(cam.height, r0 + rows_per_step)), seed=step)
+        if step >= args.warmup:
+            times.append(dt)
+            rays_total += rays
+    value = rays_total / sum(times) / 1e6
+    sample = f"{args.workload} rows of {rows_per_step} x {cam.width} px x {p['spp']} spp per step"
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (procedural scene, seeded)", "config": {"workload": text},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cfg1", choices=["cfg1", "cfg0"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traverse", default="fast", choices=["fast", "ref"])
+    ap.add_argument("--res", type=int, default=0, help="override the resolution (profiling small cases)")
+    ap.add_argument("--spp", type=int, default=0, help="override spp (profiling small cases)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+        td.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import mcrt_gb300
+    from mcrt_gb300 import GpuScene, TRAVERSE_FAST, TRAVERSE_REF
+    from mcrt_gb300._native import PROFILE_COUNT, PROFILE_STAGES
+
+    mcrt_gb300.load()
+    desc, cam, p, text = workload(args.workload)
+    if args.res:
+        cam.width = cam.height = args.res
+        text += f" [reduced: {args.res}x{args.res}]"
+    if args.spp:
+        p["spp"] = args.spp
+        text += f" [reduced: {args.spp} spp]"
+    t0 = time.time()
+    sc = GpuScene(desc)
+    setup_s = time.time() - t0
+    traverse = TRAVERSE_FAST if args.traverse == "fast" else TRAVERSE_REF
+    out = torch.empty((cam.height, cam.width, 3), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    kw = dict(spp=p["spp"], max_depth=p["max_depth"], rr_depth=p["rr_depth"], traverse=traverse)
+
+    def barrier():
+        if dist:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for w in range(args.warmup):
+        sc.render(cam, seed=100 + w, out=out, profile=PROFILE_STAGES, **kw)
+    # timed region: one render per step, stage events inside, L2 flushed between steps
+    step_ms, rays, paths, extend_ms, extend_launches = [], 0, 0, 0.0, 0
+    st_last = None
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _, st = sc.render(cam, seed=k, out=out, profile=PROFILE_STAGES, **kw)
+            e1.record()
+            barrier()
+            step_ms.append(e0.elapsed_time(e1))
+            rays += st["rays"]
+            paths += st["paths"]
+            extend_ms += st["stage_ms"][1]
+            extend_launches += st["extend_launches"]
+            st_last = st
+    clocks = clk.summary()
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        r = torch.tensor([float(rays), float(paths)], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(r)
+        rays, paths = int(r[0].item()), int(r[1].item())
+    value = rays / (total_ms / 1e3) / 1e6
+    msamples = paths / (total_ms / 1e3) / 1e6
+
+    # algorithmic bytes of the extension traversal: a counting render of the same seeds
+    _, sc_cnt = sc.render(cam, seed=0, out=out, profile=PROFILE_COUNT, **kw)
+    ext_bytes = 64 * sc_cnt["ext_nodes"] + 48 * sc_cnt["ext_tris"] + (32 + 16) * sc_cnt["extension_rays"]
+    per_launch_bytes = ext_bytes / max(st_last["extend_launches"], 1)
+    avg_launch_ms = extend_ms / max(extend_launches, 1)
+    achieved = per_launch_bytes / (avg_launch_ms / 1e3) / 1e9 if avg_launch_ms > 0 else 0.0
+    peak, peak_kind = measured_peak_hbm()
+
+    # e2e: the C-ABI call with host buffers (image copied back inside the call)
+    host_img = np.zeros((cam.height, cam.width, 3), np.float32)
+    e2e_ms, e2e_rays, h2d, d2h = [], 0, 0, 0
+    for k in range(max(1, args.steps)):
+        flush.zero_()
+        barrier()
+        t0 = time.perf_counter()
+        _, st = sc.render(cam, seed=k, out=host_img, **kw)
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+        e2e_rays += st["rays"]
+        h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+    e2e_value = e2e_rays / (sum(e2e_ms) / 1e3) / 1e6 * (world if dist else 1)
+
+    # launches of our kernels inside the timed region
+    launches = st_last["kernel_launches"] * args.steps
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rows = {"cfg0": (96, 160), "cfg1": (448, 480)}[args.workload]
+        c_rays, c_paths, c_dt, c_build = cpu_port_sample(desc, cam, p, rows)
+        cpu = {"value": round(c_rays / c_dt / 1e6, 3), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{args.workload} rows {rows[0]}-{rows[1]} x {cam.width} px x {p['spp']} spp "
+                         f"({c_paths} paths, {c_dt:.1f} s; float port of the estimator)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scene, seeded)",
+            "config": {"workload": text, "traversal": args.traverse, "l2": "flushed between steps (256 MB write)",
+                       "parallelism": f"replicas x{world}", "waves_per_step": st_last["waves"],
+                       "scene_setup_s": round(setup_s, 2)},
+            "msamples_per_s": round(msamples, 3),
+            "rays_per_path": round(rays / max(paths, 1), 3),
+            "roofline": {"bound": "hbm", "kernel": "k_extend (closest-hit traversal)", "achieved": round(achieved, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                         "peak_source": peak_kind,
+                         "bytes_per_ray": round(ext_bytes / max(sc_cnt["extension_rays"], 1), 1),
+                         "nodes_per_ray": round(sc_cnt["ext_nodes"] / max(sc_cnt["extension_rays"], 1), 2),
+                         "tris_per_ray": round(sc_cnt["ext_tris"] / max(sc_cnt["extension_rays"], 1), 2),
+                         "extend_share_of_step": round(extend_ms / max(total_ms, 1e-9), 3)},
+            "stage_ms_per_step": [round(x, 2) for x in st_last["stage_ms"]],
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

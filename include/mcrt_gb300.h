@@ -138,7 +138,11 @@ typedef struct mcrt_render_params {
     int64_t  path_chunk;  /* paths in flight per wave, 0 -> library default */
     int32_t  block_size;  /* threads per block of the wavefront kernels, 0 -> default */
     int32_t  use_graph;   /* capture each wave's per-stage kernels in a CUDA graph */
+    int32_t  profile;     /* MCRT_PROFILE_* bits (diagnostics; off for production renders) */
 } mcrt_render_params;
+
+#define MCRT_PROFILE_STAGES 1 /* CUDA events around every stage launch -> stats.stage_ms */
+#define MCRT_PROFILE_COUNT 2  /* count BVH nodes fetched / triangles tested per ray class */
 
 typedef struct mcrt_render_stats {
     int64_t paths;
@@ -146,7 +150,15 @@ typedef struct mcrt_render_stats {
     int64_t shadow_rays;
     int32_t waves;
     int32_t kernel_launches;
-    float   device_ms; /* CUDA-event time of the kernels (excludes host copies) */
+    float   device_ms;   /* CUDA-event time of the kernels (excludes host copies) */
+    float   stage_ms[4]; /* MCRT_PROFILE_STAGES: begin+raygen, extend, shade, connect+resolve */
+    int32_t extend_launches;
+    int64_t ext_nodes;   /* MCRT_PROFILE_COUNT: nodes fetched / triangles tested by extension */
+    int64_t ext_tris;    /* rays, and by next-event rays */
+    int64_t nee_nodes;
+    int64_t nee_tris;
+    int64_t h2d_bytes;   /* host -> device bytes copied by the call (tables, host inputs) */
+    int64_t d2h_bytes;   /* device -> host bytes copied by the call (host outputs, status) */
 } mcrt_render_stats;
 
 int         mcrt_get_abi_version(void);

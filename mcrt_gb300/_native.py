@@ -27,6 +27,8 @@ TRAVERSE_FAST = 0
 TRAVERSE_REF = 1
 PTR_HOST = 0
 PTR_DEVICE = 1
+PROFILE_STAGES = 1
+PROFILE_COUNT = 2
 BUILD_SAH = 0
 BUILD_EXTERNAL = 1
 
@@ -64,12 +66,14 @@ class Camera(ctypes.Structure):
 class RenderParams(ctypes.Structure):
     _fields_ = [("spp", c_int32), ("max_depth", c_int32), ("rr_depth", c_int32), ("seed", ctypes.c_uint64),
                 ("traverse", c_int32), ("ptr_mode", c_int32), ("path_chunk", c_int64), ("block_size", c_int32),
-                ("use_graph", c_int32)]
+                ("use_graph", c_int32), ("profile", c_int32)]
 
 
 class RenderStats(ctypes.Structure):
     _fields_ = [("paths", c_int64), ("extension_rays", c_int64), ("shadow_rays", c_int64), ("waves", c_int32),
-                ("kernel_launches", c_int32), ("device_ms", c_float)]
+                ("kernel_launches", c_int32), ("device_ms", c_float), ("stage_ms", c_float * 4),
+                ("extend_launches", c_int32), ("ext_nodes", c_int64), ("ext_tris", c_int64), ("nee_nodes", c_int64),
+                ("nee_tris", c_int64), ("h2d_bytes", c_int64), ("d2h_bytes", c_int64)]
 
 
 EXPORTS = {

@@ -164,9 +164,15 @@ __device__ __forceinline__ bool watertight(const WatertightRay& r, float3 v0, fl
 
 // Two-child traversal over FastNode with a per-thread stack in shared memory
 // (`stack` points at this thread's column, entries `stride` ints apart).
-template <bool ANY, int STACK>
+// Work counters of a traversal (MCRT_PROFILE_COUNT): nodes fetched, triangles tested.
+struct TraceCount
+{
+    unsigned nodes, tris;
+};
+
+template <bool ANY, int STACK, bool COUNT = false>
 __device__ __forceinline__ bool trace_fast(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
-                                           int* stack, int stride, Hit& hit, int* err)
+                                           int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr)
 {
     const float big = 1e30f;
     float3      inv = mk(fabsf(d.x) > 1e-30f ? 1.0f / d.x : copysignf(big, d.x),
@@ -185,6 +191,7 @@ __device__ __forceinline__ bool trace_fast(const SceneView& s, float3 o, float3 
         while (cur >= 0 && cur != kSentinel)
         {
             const float4* np = reinterpret_cast<const float4*>(s.fast_nodes + cur);
+            if (COUNT) cnt->nodes++;
             float4        n0 = __ldg(np + 0);
             float4        n1 = __ldg(np + 1);
             float4        n2 = __ldg(np + 2);
@@ -234,6 +241,7 @@ __device__ __forceinline__ bool trace_fast(const SceneView& s, float3 o, float3 
         {
             int code = ~cur;
             int first = code >> 4, count = code & 15;
+            if (COUNT) cnt->tris += count;
             for (int k = 0; k < count; ++k)
             {
                 const float4* tp = s.fast_tris + 3 * (first + k);
@@ -403,12 +411,12 @@ __device__ __forceinline__ bool trace_ref(const SceneView& s, float3 o, float3 d
     return hit.prim >= 0;
 }
 
-template <bool ANY, int STACK>
+template <bool ANY, int STACK, bool COUNT = false>
 __device__ __forceinline__ bool trace_ray(const SceneView& s, int mode, float3 o, float3 d, float tmin, float tmax,
-                                          int* stack, int stride, Hit& hit, int* err)
+                                          int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr)
 {
     if (mode == 1) return trace_ref<ANY, STACK>(s, o, d, tmin, tmax, stack, stride, hit, err);
-    bool found = trace_fast<ANY, STACK>(s, o, d, tmin, tmax, stack, stride, hit, err);
+    bool found = trace_fast<ANY, STACK, COUNT>(s, o, d, tmin, tmax, stack, stride, hit, err, cnt);
     if (!ANY && found)
     {
         // The watertight test decides which triangle is closest; the reported t, u, v

@@ -27,6 +27,7 @@
 
 #include "../../include/mcrt_gb300.h"
 #include "device.cuh"
+#include "estimator.cuh"
 #include "host.h"
 
 namespace mcrt {
@@ -71,13 +72,6 @@ struct Ctrl
     int     scount[kMaxDepth + 1][2];
 };
 
-enum ShadowType
-{
-    SH_ENV = 0,
-    SH_AREA_BSDF = 1,
-    SH_AREA_LIGHT = 2
-};
-
 struct WaveArgs
 {
     Ctrl*               ctrl;
@@ -94,14 +88,32 @@ struct WaveArgs
     uint64_t*           rng;
     int*                pix;
     int*                job;
+    float4*             nee_val;  // 4 next-event results per path slot (written by k_connect)
+    int*                pend;     // per path slot: mask of next-event results not yet added
     float4*             so[2];  // [0] any-hit queue, [1] closest-hit queue
     float4*             sd[2];
     float4*             sv[2];
     int4*               sm[2];
     int64_t             shadow_cap;
-    unsigned long long* stats;  // [0] extension rays, [1] shadow rays
+    unsigned long long* stats;  // [0] extension rays, [1] shadow rays, [2..5] work counters
     int*                err;
 };
+
+// warp-reduced add of per-thread work counters into stats[slot], stats[slot + 1]
+__device__ __forceinline__ void flush_count(unsigned long long* stats, int slot, const TraceCount& c)
+{
+    unsigned long long nn = c.nodes, tt = c.tris;
+    for (int off = 16; off > 0; off >>= 1)
+    {
+        nn += __shfl_down_sync(0xffffffffu, nn, off);
+        tt += __shfl_down_sync(0xffffffffu, tt, off);
+    }
+    if ((threadIdx.x & 31) == 0 && (nn | tt))
+    {
+        atomicAdd(&stats[slot], nn);
+        atomicAdd(&stats[slot + 1], tt);
+    }
+}
 
 __device__ __forceinline__ int find_job(const JobGPU* jobs, int num_jobs, int64_t g)
 {
@@ -163,16 +175,33 @@ __global__ void k_raygen(WaveArgs a)
         a.rng[p] = rng.state;
         a.pix[p] = pixel;
         a.job[p] = j;
+        a.pend[p] = 0;
     }
 }
 
-template <int STACK>
+// adds a path's pending next-event results in slot order (deterministic sum)
+__device__ __forceinline__ float4 add_pending(const WaveArgs& a, int p, float4 r)
+{
+    int m = a.pend[p];
+    for (int s = 0; s < 4; ++s)
+        if (m & (1 << s))
+        {
+            float4 v = a.nee_val[4 * p + s];
+            r.x += v.x;
+            r.y += v.y;
+            r.z += v.z;
+        }
+    return r;
+}
+
+template <int STACK, bool COUNT>
 __global__ void __launch_bounds__(kTraceBlock) k_extend(WaveArgs a, int depth)
 {
     __shared__ int stack[STACK * kTraceBlock];
     int*           st = stack + threadIdx.x;
     const int      n = a.ctrl->qcount[depth];
     const int      qs = depth & 1;
+    TraceCount     cnt = {0u, 0u};
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[0], static_cast<unsigned long long>(n));
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
@@ -180,11 +209,12 @@ __global__ void __launch_bounds__(kTraceBlock) k_extend(WaveArgs a, int depth)
         int    p = a.qp[qs][i];
         int    j = a.job[p];
         Hit    h;
-        bool   hit = trace_ray<false, STACK>(a.jobs[j].scene, a.jobs[j].traverse, xyz(o), xyz(d), o.w, d.w, st,
-                                           kTraceBlock, h, a.err);
+        bool   hit = trace_ray<false, STACK, COUNT>(a.jobs[j].scene, a.jobs[j].traverse, xyz(o), xyz(d), o.w, d.w,
+                                                  st, kTraceBlock, h, a.err, &cnt);
         a.hits[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.prim))
                         : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
     }
+    if (COUNT) flush_count(a.stats, 2, cnt);
 }
 
 __device__ __forceinline__ unsigned lanemask_lt()
@@ -212,14 +242,6 @@ __device__ __forceinline__ int warp_append(int* counter, int k)
     return base + incl - k;
 }
 
-struct ShadowRay
-{
-    float3 d;
-    float  tmax;
-    float4 val;
-    int    type, light;
-};
-
 __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
 {
     const int n = a.ctrl->qcount[depth];
@@ -230,32 +252,29 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
     {
         int  i = wbase + lane;
         bool valid = i < n;
-        // outputs of this lane
-        bool      cont = false;
-        float3    phit = mk(0.f, 0.f, 0.f), cdir = mk(0.f, 0.f, 1.f);
-        float3    T2 = mk(0.f, 0.f, 0.f);
-        int       flags2 = 0;
-        ShadowRay sh_any[2], sh_cl[2];
-        int       n_any = 0, n_cl = 0;
-        int       p = 0;
-        uint64_t  rstate = 0;
+        bool     cont = false;
+        float3   phit = mk(0.f, 0.f, 0.f), cdir = mk(0.f, 0.f, 1.f), T2 = mk(0.f, 0.f, 0.f);
+        int      flags2 = 0, n_nee = 0, p = 0;
+        uint64_t rstate = 0;
+        NeeRay   nee[4];
         if (valid)
         {
-            float4        o4 = a.qo[qs][i], d4 = a.qd[qs][i];
-            float4        hh = a.hits[i];
-            float3        o = xyz(o4), d = xyz(d4);
+            float4           o4 = a.qo[qs][i], d4 = a.qd[qs][i];
+            float4           hh = a.hits[i];
+            float3           o = xyz(o4), d = xyz(d4);
             p = a.qp[qs][i];
-            const JobGPU& J = a.jobs[a.job[p]];
+            const JobGPU&    J = a.jobs[a.job[p]];
             const SceneView& S = J.scene;
-            float4        t4 = a.thr[p];
-            float3        T = xyz(t4);
-            int           flags = __float_as_int(t4.w);
-            bool          no_direct = depth == 0 || !(flags & 1);
-            int           prim = __float_as_int(hh.w);
-            float3        Ladd = mk(0.f, 0.f, 0.f);
+            float4           t4 = a.thr[p];
+            float3           T = xyz(t4);
+            bool             no_direct = depth == 0 || !(__float_as_int(t4.w) & 1);
+            int              prim = __float_as_int(hh.w);
+            float3           Ladd = mk(0.f, 0.f, 0.f);
+            // results of the previous vertex's next-event rays first, then this vertex
+            float4 rp = add_pending(a, p, a.rad[p]);
             if (prim < 0)
             {
-                if (no_direct && S.env_w > 0) Ladd = T * env_radiance(S, d);
+                Ladd = miss_emission(S, d, T, no_direct);
             }
             else
             {
@@ -277,132 +296,16 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
                     for (int k = 0; k < NUM_DIMS; ++k) u[k] = rng.uniform();
                     rstate = rng.state;
                     float3 wi = -d;
-                    bool   nee = does_nee(m.type);
-                    if (nee)
-                    {
-                        if (S.env_w > 0)
-                        {
-                            // sampleEnvmapUsingLightPDF (demo_pt.cpp:430-465)
-                            float3 ldir, lrad;
-                            float  lpdf;
-                            env_sample(S, u[D_ENV_LIGHT_0], u[D_ENV_LIGHT_1], u[D_ENV_JITTER_U], u[D_ENV_JITTER_V],
-                                       ldir, lrad, lpdf);
-                            float g = fmax_ref(0.f, dot3(ldir, ns));
-                            if (g > 0.f)
-                            {
-                                float  pe = env_pdf(S, ldir);
-                                float  wE = pe / (pe + bsdf_pdf(m, wi, ns, ldir));
-                                float3 irr = (bsdf_eval(m, wi, ns, ldir) * g * (1.0f / lpdf)) * lrad;
-                                float3 val = T * (irr * wE);
-                                if (!isnan3(val))
-                                    sh_any[n_any++] = ShadowRay{ldir, __int_as_float(0x7f800000),
-                                                                make_float4(val.x, val.y, val.z, 0.f), SH_ENV, 0};
-                            }
-                            // sampleEnvmapUsingSurfacePDF (demo_pt.cpp:466-507); GGX samples itself
-                            if (m.type == MAT_DIFF)
-                            {
-                                float  r1 = 2.f * kPi * u[D_ENV_BSDF_0], r2 = u[D_ENV_BSDF_1], r2s = sqrtf(r2);
-                                float3 w = ns;
-                                float3 uu = normalize3(cross3(mk(0.3f, 0.4f, 0.5f), w));
-                                float3 vv = cross3(w, uu);
-                                float3 wo = normalize3(uu * (cosf(r1) * r2s) + vv * (sinf(r1) * r2s) + w * sqrtf(1.f - r2));
-                                float  g2 = fmax_ref(0.f, dot3(wo, ns));
-                                if (g2 > 0.f)
-                                {
-                                    float  pb = bsdf_pdf(m, wi, ns, wo);
-                                    float  wB = pb / (pb + env_pdf(S, wo));
-                                    float3 val = T * ((m.color * env_radiance(S, wo)) * wB);
-                                    if (!isnan3(val))
-                                        sh_any[n_any++] = ShadowRay{wo, __int_as_float(0x7f800000),
-                                                                    make_float4(val.x, val.y, val.z, 0.f), SH_ENV, 0};
-                                }
-                            }
-                            else
-                            {
-                                BsdfSample bs = bsdf_sample(m, wi, ns, u[D_ENV_BSDF_0], u[D_ENV_BSDF_1]);
-                                if (maxc(bs.weight) > 0.f && bs.pdf > 0.f)
-                                {
-                                    float  wB = bs.pdf / (bs.pdf + env_pdf(S, bs.wo));
-                                    float3 val = T * ((bs.weight * env_radiance(S, bs.wo)) * wB);
-                                    if (!isnan3(val))
-                                        sh_any[n_any++] = ShadowRay{bs.wo, __int_as_float(0x7f800000),
-                                                                    make_float4(val.x, val.y, val.z, 0.f), SH_ENV, 0};
-                                }
-                            }
-                        }
-                        if (S.light_area > 0.f)
-                        {
-                            // BSDF sample with MIS (demo_pt.cpp:593-614)
-                            BsdfSample bs = bsdf_sample(m, wi, ns, u[D_AREA_BSDF_0], u[D_AREA_BSDF_1]);
-                            if (maxc(bs.weight) > 0.f)
-                            {
-                                float3 val = T * bs.weight;
-                                sh_cl[n_cl++] = ShadowRay{bs.wo, __int_as_float(0x7f800000),
-                                                          make_float4(val.x, val.y, val.z, bs.pdf), SH_AREA_BSDF, 0};
-                            }
-                            // light sample (demo_pt.cpp:618-641; scene.cpp:298-343)
-                            int lo = 0, hi = S.num_lights - 1;
-                            while (hi > lo)
-                            {
-                                int mid = lo + (hi - lo) / 2;
-                                if (S.lights[mid].cdf >= u[D_LIGHT_PICK])
-                                    hi = mid;
-                                else
-                                    lo = mid + 1;
-                            }
-                            LightGPU      L = S.lights[lo];
-                            const float4* lv = S.prim_verts + 3 * L.prim;
-                            float         r0 = sqrtf(u[D_LIGHT_U]);
-                            float         lu = 1.f - r0, lvv = u[D_LIGHT_V] * r0;
-                            float3 lp = xyz(lv[0]) * (1.f - lu - lvv) + xyz(lv[1]) * lu + xyz(lv[2]) * lvv;
-                            int    lm;
-                            float3 ln = shading_normal(S, L.prim, lu, lvv, lm);
-                            float  pdfA = (1.f / L.area) * L.pdf;
-                            float3 wo = lp - phit;
-                            float  dist2 = dot3(wo, wo);
-                            wo = normalize3(wo);
-                            float cosl = dot3(ln, -wo);
-                            float pdfW = pdfA * dist2 / fabsf(cosl);
-                            if (cosl <= 0.f) pdfW = 0.f;
-                            if (pdfW > 0.f)
-                            {
-                                float  pb = bsdf_pdf(m, wi, ns, wo);
-                                float  mis = pdfW / (pdfW + pb);
-                                float3 f = bsdf_eval(m, wi, ns, wo);
-                                float  cs = fmaxf(dot3(ns, wo), 0.f);
-                                if (maxc(f) > 0.f && cs > 0.f)
-                                {
-                                    float3 val = T * (f * (cs / pdfW * mis));
-                                    sh_cl[n_cl++] = ShadowRay{wo, sqrtf(dist2) * 1.001f + kEpsRay,
-                                                              make_float4(val.x, val.y, val.z, 0.f), SH_AREA_LIGHT, lo};
-                                }
-                            }
-                        }
-                    }
-                    // continuation (demo_pt.cpp:647-650) and Russian roulette
-                    BsdfSample cs = bsdf_sample(m, wi, ns, u[D_CONT_0], u[D_CONT_1]);
-                    T2 = T * cs.weight;
-                    cont = depth < J.max_depth;
-                    if (J.rr_depth >= 0 && depth >= J.rr_depth)
-                    {
-                        float q = fminf(fmaxf(maxc(m.color), 0.f), 1.f);
-                        if (u[D_RR] >= q)
-                            cont = false;
-                        else
-                            T2 = T2 * (1.f / q);
-                    }
-                    if (!(maxc(T2) > 0.f)) cont = false;
-                    cdir = cs.wo;
-                    flags2 = nee ? 1 : 0;
+                    bool   nee_here = does_nee(m.type);
+                    if (nee_here) n_nee = make_nee(S, m, wi, ns, phit, T, u, nee);
+                    cont = continue_path(m, wi, ns, T, u, depth, J.max_depth, J.rr_depth, T2, cdir);
+                    flags2 = nee_here ? 1 : 0;
                 }
             }
-            if (Ladd.x != 0.f || Ladd.y != 0.f || Ladd.z != 0.f)
-            {
-                float4 r = a.rad[p];
-                a.rad[p] = make_float4(r.x + Ladd.x, r.y + Ladd.y, r.z + Ladd.z, r.w);
-            }
+            a.rad[p] = make_float4(rp.x + Ladd.x, rp.y + Ladd.y, rp.z + Ladd.z, rp.w);
+            a.pend[p] = (1 << n_nee) - 1;
         }
-        // compaction of live paths into the next queue (ballot + popc)
+        // compaction of live paths into the next queue (ballot + popc, one atomic per warp)
         unsigned live = __ballot_sync(0xffffffffu, cont);
         if (live)
         {
@@ -427,87 +330,236 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
                 }
             }
         }
-        // shadow rays (warp prefix sum + one atomic per warp and queue)
+        // next-event rays: any-hit queue [0], closest-hit queue [1] (warp prefix sums)
+        int n_any = 0;
+        for (int r = 0; r < n_nee; ++r) n_any += nee[r].type == NEE_ENV ? 1 : 0;
+        int n_cl = n_nee - n_any;
         for (int qsel = 0; qsel < 2; ++qsel)
         {
             int k = qsel == 0 ? n_any : n_cl;
             int b = warp_append(&a.ctrl->scount[depth][qsel], k);
-            for (int r = 0; r < 2; ++r)
+            int w = 0;
+            for (int r = 0; r < n_nee; ++r)
             {
-                if (r >= k) break;
-                const ShadowRay& sr = qsel == 0 ? sh_any[r] : sh_cl[r];
-                int              idx = b + r;
+                if ((nee[r].type == NEE_ENV) != (qsel == 0)) continue;
+                int idx = b + w++;
                 if (idx >= a.shadow_cap)
                 {
                     atomicOr(a.err, kErrQueue);
                     break;
                 }
                 a.so[qsel][idx] = make_float4(phit.x, phit.y, phit.z, kEpsRay);
-                a.sd[qsel][idx] = make_float4(sr.d.x, sr.d.y, sr.d.z, sr.tmax);
-                a.sv[qsel][idx] = sr.val;
-                a.sm[qsel][idx] = make_int4(p, sr.type, sr.light, 0);
+                a.sd[qsel][idx] = make_float4(nee[r].d.x, nee[r].d.y, nee[r].d.z, nee[r].tmax);
+                a.sv[qsel][idx] = nee[r].val;
+                a.sm[qsel][idx] = make_int4(p, nee[r].type, nee[r].light, r);
             }
         }
     }
 }
 
-template <int STACK>
+template <int STACK, bool COUNT>
 __global__ void __launch_bounds__(kTraceBlock) k_connect(WaveArgs a, int depth)
 {
     __shared__ int stack[STACK * kTraceBlock];
     int*           st = stack + threadIdx.x;
+    TraceCount     cnt = {0u, 0u};
     const int      n0 = a.ctrl->scount[depth][0];
     const int      n1 = a.ctrl->scount[depth][1];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[1], static_cast<unsigned long long>(n0 + n1));
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0 + n1; i += gridDim.x * blockDim.x)
     {
-        int    q = i < n0 ? 0 : 1;
-        int    k = i < n0 ? i : i - n0;
-        float4 o = a.so[q][k], d = a.sd[q][k], v = a.sv[q][k];
-        int4   m = a.sm[q][k];
-        int    p = m.x;
+        int              q = i < n0 ? 0 : 1;
+        int              k = i < n0 ? i : i - n0;
+        float4           o = a.so[q][k], d = a.sd[q][k], v = a.sv[q][k];
+        int4             m = a.sm[q][k];
+        int              p = m.x;
         const JobGPU&    J = a.jobs[a.job[p]];
         const SceneView& S = J.scene;
         Hit              h;
-        float3           add = mk(0.f, 0.f, 0.f);
-        if (q == 0)
+        bool hit = q == 0 ? trace_ray<true, STACK, COUNT>(S, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock, h,
+                                                          a.err, &cnt)
+                          : trace_ray<false, STACK, COUNT>(S, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock,
+                                                           h, a.err, &cnt);
+        float3 coef;
+        int    emat;
+        float3 add = nee_contribution(S, m.y, m.z, v, xyz(d), hit, h, coef, emat);
+        a.nee_val[4 * p + m.w] = make_float4(add.x, add.y, add.z, 0.f);
+    }
+    if (COUNT) flush_count(a.stats, 4, cnt);
+}
+
+// ---------------------------------------------------------------------------
+// path-replay adjoint (Vicini et al. 2021): each path is re-traced from its seed and
+// differentiated on the fly; nothing is taped, memory is O(pixels + parameters).
+// The radiance of a path is multilinear in the Lambert albedos and the emitter
+// radiances of the vertices it visits:
+//   d L / d albedo_k = (L - L_before(k)) / albedo_k, summed over the vertices k that use
+//                      that albedo (L_before: radiance gathered before vertex k);
+//   d L / d E        = the coefficient multiplying E in each emission term.
+// Russian-roulette probabilities are held constant (their derivative has zero mean).
+// ---------------------------------------------------------------------------
+struct AdjointArgs
+{
+    JobGPU       job;
+    const float* dLdI;  // [H][W][3]
+    float*       g_albedo;
+    int          n_albedo;
+    float*       g_emis;
+    int          n_emis;
+    int          shared_grads;  // accumulate in shared memory, flush once per block
+    int64_t      total_paths;
+    unsigned long long* stats;
+    int*         err;
+};
+
+constexpr int kAdjBlock = 64;
+constexpr int kMaxLog = kMaxDepth + 2;
+
+template <int STACK>
+__global__ void __launch_bounds__(kAdjBlock) k_adjoint(AdjointArgs a)
+{
+    extern __shared__ float sgrad[];  // (n_albedo + n_emis) * 3 when shared_grads
+    __shared__ int          stack[STACK * kAdjBlock];
+    int*                    st = stack + threadIdx.x;
+    const int               ng = (a.n_albedo + a.n_emis) * 3;
+    if (a.shared_grads)
+        for (int k = threadIdx.x; k < ng; k += blockDim.x) sgrad[k] = 0.f;
+    __syncthreads();
+    float* ga = a.shared_grads ? sgrad : a.g_albedo;
+    float* ge = a.shared_grads ? sgrad + 3 * a.n_albedo : a.g_emis;
+    const JobGPU&    J = a.job;
+    const SceneView& S = J.scene;
+    unsigned long long rays = 0;
+    for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < a.total_paths;
+         g += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        int pixel = static_cast<int>(g / J.spp);
+        int s = static_cast<int>(g - static_cast<int64_t>(pixel) * J.spp);
+        int x = pixel % J.width, y = pixel / J.width;
+        Pcg rng;
+        rng.seed(J.seed, static_cast<uint32_t>(pixel), static_cast<uint32_t>(s));
+        float r1 = 2.f * rng.uniform();
+        float r2 = 2.f * rng.uniform();
+        float dx = J.spp > 1 ? tent(r1) : 0.f, dy = J.spp > 1 ? tent(r2) : 0.f;
+        float3 o, d;
+        camera_ray(J.cam, (static_cast<float>(x) + 0.5f + dx) / static_cast<float>(J.width),
+                   (static_cast<float>(y) + 0.5f + dy) / static_cast<float>(J.height), o, d);
+        float3 dl = mk(a.dLdI[3 * pixel], a.dLdI[3 * pixel + 1], a.dLdI[3 * pixel + 2]) * (1.0f / J.spp);
+        float3 L = mk(0.f, 0.f, 0.f), T = mk(1.f, 1.f, 1.f);
+        bool   last_nee = false;
+        // per-vertex log for the albedo adjoint
+        int    lparam[kMaxLog];
+        float3 lalb[kMaxLog], lbefore[kMaxLog];
+        int    nlog = 0;
+        for (int depth = 0; depth <= J.max_depth; ++depth)
         {
-            if (!trace_ray<true, STACK>(S, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock, h, a.err))
-                add = xyz(v);
-        }
-        else if (trace_ray<false, STACK>(S, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock, h, a.err))
-        {
-            int    matid;
-            float3 dir = xyz(d);
-            float3 ns = shading_normal(S, h.prim, h.u, h.v, matid);
-            Mat    hm = load_mat(S, matid);
-            if (hm.type == MAT_LGHT && !(dot3(ns, -dir) < 0.f))
+            Hit  h;
+            bool hit = trace_ray<false, STACK>(S, J.traverse, o, d, kEpsRay, __int_as_float(0x7f800000), st, kAdjBlock,
+                                               h, a.err);
+            ++rays;
+            bool no_direct = depth == 0 || !last_nee;
+            if (!hit)
             {
-                if (m.y == SH_AREA_BSDF)
+                L = L + miss_emission(S, d, T, no_direct);
+                break;
+            }
+            int    matid;
+            float3 ns = shading_normal(S, h.prim, h.u, h.v, matid);
+            Mat    m = load_mat(S, matid);
+            float3 phit = o + d * h.t;
+            if (m.type == MAT_LGHT)
+            {
+                if (no_direct && dot3(d, ns) < 0.f)
                 {
-                    // Scene::lightPdfW (scene.cpp:239-267) + lightRadiance (:345-366)
-                    float cl = dot3(ns, -dir);
-                    float pdfL = 0.f;
-                    if (cl >= 1e-6f)
+                    L = L + T * m.color;
+                    if (m.emission_param >= 0 && m.emission_param < a.n_emis)
                     {
-                        LightGPU L = S.lights[S.light_of[h.prim]];
-                        float    pdfA = (1.f / L.area) * L.pdf;
-                        pdfL = pdfA * (h.t * h.t) / cl;
+                        float3 c = T * dl;
+                        atomicAdd(&ge[3 * m.emission_param + 0], c.x);
+                        atomicAdd(&ge[3 * m.emission_param + 1], c.y);
+                        atomicAdd(&ge[3 * m.emission_param + 2], c.z);
                     }
-                    float mis = v.w / (v.w + pdfL);
-                    add = xyz(v) * hm.color * mis;
                 }
-                else if (S.light_of[h.prim] == m.z)
+                break;
+            }
+            float u[NUM_DIMS];
+#pragma unroll
+            for (int k = 0; k < NUM_DIMS; ++k) u[k] = rng.uniform();
+            float3 wi = -d;
+            bool   nee_here = does_nee(m.type);
+            float3 before = L;
+            if (nee_here)
+            {
+                NeeRay nee[4];
+                int    nn = make_nee(S, m, wi, ns, phit, T, u, nee);
+                for (int r = 0; r < nn; ++r)
                 {
-                    add = xyz(v) * hm.color;
+                    Hit  hs;
+                    bool any = nee[r].type == NEE_ENV;
+                    bool hh = any ? trace_ray<true, STACK>(S, J.traverse, phit, nee[r].d, kEpsRay, nee[r].tmax, st,
+                                                          kAdjBlock, hs, a.err)
+                                  : trace_ray<false, STACK>(S, J.traverse, phit, nee[r].d, kEpsRay, nee[r].tmax, st,
+                                                           kAdjBlock, hs, a.err);
+                    ++rays;
+                    float3 coef;
+                    int    emat;
+                    float3 add = nee_contribution(S, nee[r].type, nee[r].light, nee[r].val, nee[r].d, hh, hs, coef, emat);
+                    L = L + add;
+                    if (emat >= 0)
+                    {
+                        int ep = S.materials[emat].emission_param;
+                        if (ep >= 0 && ep < a.n_emis)
+                        {
+                            float3 c = coef * dl;
+                            atomicAdd(&ge[3 * ep + 0], c.x);
+                            atomicAdd(&ge[3 * ep + 1], c.y);
+                            atomicAdd(&ge[3 * ep + 2], c.z);
+                        }
+                    }
                 }
             }
+            if (m.type == MAT_DIFF && m.albedo_param >= 0 && m.albedo_param < a.n_albedo && nlog < kMaxLog)
+            {
+                lparam[nlog] = m.albedo_param;
+                lalb[nlog] = m.color;
+                lbefore[nlog] = before;
+                ++nlog;
+            }
+            float3 T2, cdir;
+            bool   cont = continue_path(m, wi, ns, T, u, depth, J.max_depth, J.rr_depth, T2, cdir);
+            last_nee = nee_here;
+            if (!cont) break;
+            T = T2;
+            o = phit;
+            d = cdir;
         }
-        if (add.x != 0.f || add.y != 0.f || add.z != 0.f)
+        if (isnan3(L)) continue;  // demo_pt.cpp:653 scrubs the path to zero: no gradient
+        for (int k = 0; k < nlog; ++k)
         {
-            atomicAdd(&a.rad[p].x, add.x);
-            atomicAdd(&a.rad[p].y, add.y);
-            atomicAdd(&a.rad[p].z, add.z);
+            float3 Sk = L - lbefore[k];
+            float3 al = lalb[k];
+            int    pk = lparam[k];
+            if (al.x > 0.f) atomicAdd(&ga[3 * pk + 0], dl.x * Sk.x / al.x);
+            if (al.y > 0.f) atomicAdd(&ga[3 * pk + 1], dl.y * Sk.y / al.y);
+            if (al.z > 0.f) atomicAdd(&ga[3 * pk + 2], dl.z * Sk.z / al.z);
+        }
+    }
+    // warp-reduced ray count
+    for (int off = 16; off > 0; off >>= 1) rays += __shfl_down_sync(0xffffffffu, rays, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&a.stats[0], rays);
+    if (a.shared_grads)
+    {
+        __syncthreads();
+        for (int k = threadIdx.x; k < ng; k += blockDim.x)
+        {
+            float v = sgrad[k];
+            if (v != 0.f)
+            {
+                if (k < 3 * a.n_albedo)
+                    atomicAdd(&a.g_albedo[k], v);
+                else
+                    atomicAdd(&a.g_emis[k - 3 * a.n_albedo], v);
+            }
         }
     }
 }
@@ -527,7 +579,7 @@ __global__ void k_resolve(WaveArgs a)
         float s[3] = {0.f, 0.f, 0.f};
         for (int k = 0; k < J.spp; ++k)
         {
-            float4 r = a.rad[p + k];
+            float4 r = add_pending(a, p + k, a.rad[p + k]);
             if (isnan3(xyz(r))) r = make_float4(0.f, 0.f, 0.f, 0.f);  // demo_pt.cpp:653
             s[0] += fmax_ref(0.f, r.x);                                // demo_pt.cpp:703
             s[1] += fmax_ref(0.f, r.y);
@@ -699,8 +751,8 @@ int ensure_workspace(Workspace& w, int64_t capacity, int num_jobs, int64_t num_c
         int64_t C = capacity, S = 2 * capacity;
         // per-path: qo,qd x2 (64 B), qp x2 (8), hits 16, thr 16, rad 16, rng 8, pix 4, job 4
         // shadow: 2 queues x S x (so, sd, sv 48 B + sm 16 B)
-        size_t bytes = static_cast<size_t>(C) * (64 + 8 + 16 + 16 + 16 + 8 + 4 + 4) + static_cast<size_t>(S) * 2 * 64 +
-                       64 * 32;
+        size_t bytes = static_cast<size_t>(C) * (64 + 8 + 16 + 16 + 16 + 8 + 4 + 4 + 64 + 4) +
+                       static_cast<size_t>(S) * 2 * 64 + 64 * 32;
         CK(cudaMalloc(&w.block, bytes));
         char* p = static_cast<char*>(w.block);
         auto take = [&](size_t n) {
@@ -722,6 +774,8 @@ int ensure_workspace(Workspace& w, int64_t capacity, int num_jobs, int64_t num_c
         a.rng = static_cast<uint64_t*>(take(8 * C));
         a.pix = static_cast<int*>(take(4 * C));
         a.job = static_cast<int*>(take(4 * C));
+        a.nee_val = static_cast<float4*>(take(64 * C));
+        a.pend = static_cast<int*>(take(4 * C));
         for (int k = 0; k < 2; ++k)
         {
             a.so[k] = static_cast<float4*>(take(16 * S));
@@ -750,7 +804,7 @@ int ensure_workspace(Workspace& w, int64_t capacity, int num_jobs, int64_t num_c
     if (!w.ctrl)
     {
         CK(cudaMalloc(&w.ctrl, sizeof(Ctrl)));
-        CK(cudaMalloc(&w.stats, sizeof(unsigned long long) * 4));
+        CK(cudaMalloc(&w.stats, sizeof(unsigned long long) * 8));
         CK(cudaMalloc(&w.err, sizeof(int)));
     }
     w.args.ctrl = w.ctrl;
@@ -766,18 +820,61 @@ struct LaunchShape
     int grid_trace, grid_shade, grid_small, block;
 };
 
-template <int STACK>
-void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st)
+// Stage events: one pair per stage launch when profiling (never inside a graph).
+struct StageTimer
 {
+    std::vector<cudaEvent_t> ev;  // pairs
+    std::vector<int>         stage;
+    void record(cudaStream_t st, int stg, bool begin)
+    {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        ev.push_back(e);
+        if (begin) stage.push_back(stg);
+    }
+    void sum(float* out)
+    {
+        for (size_t k = 0; k + 1 < ev.size(); k += 2)
+        {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            out[stage[k / 2]] += ms;
+        }
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+        ev.clear();
+        stage.clear();
+    }
+};
+
+template <int STACK, bool COUNT>
+void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st, StageTimer* tm)
+{
+    auto beg = [&](int stg) {
+        if (tm) tm->record(st, stg, true);
+    };
+    auto end = [&]() {
+        if (tm) tm->record(st, 0, false);
+    };
+    beg(0);
     k_begin_chunk<<<1, 1, 0, st>>>(a);
     k_raygen<<<ls.grid_small, 256, 0, st>>>(a);
+    end();
     for (int d = 0; d <= max_depth; ++d)
     {
-        k_extend<STACK><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
+        beg(1);
+        k_extend<STACK, COUNT><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
+        end();
+        beg(2);
         k_shade<<<ls.grid_shade, 128, 0, st>>>(a, d);
-        k_connect<STACK><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
+        end();
+        beg(3);
+        k_connect<STACK, COUNT><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
+        end();
     }
+    beg(3);
     k_resolve<<<ls.grid_small, 256, 0, st>>>(a);
+    end();
 }
 
 int validate_job(const mcrt_scene* s, const mcrt_camera* c, const mcrt_render_params* p)
@@ -905,13 +1002,13 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     CK(cudaMemcpyAsync(w.jobs, jobs.data(), sizeof(JobGPU) * num_jobs, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(w.chunk_table, table.data(), sizeof(int64_t) * table.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(w.ctrl, 0, sizeof(Ctrl), st));
-    CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 4, st));
+    CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
 
     LaunchShape ls;
     int         sms = num_sms();
     int         occ_t = 0, occ_s = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend<kStack>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend<kStack, false>, kTraceBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 128, 0);
     ls.grid_trace = sms * std::max(occ_t, 1);
     ls.grid_shade = sms * std::max(occ_s, 1);
@@ -922,15 +1019,24 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     CK(cudaEventRecord(e0, st));
-    int launches = 0;
-    if (p0.use_graph)
+    int        launches = 0;
+    const bool count = (p0.profile & MCRT_PROFILE_COUNT) != 0;
+    const bool stages = (p0.profile & MCRT_PROFILE_STAGES) != 0;
+    StageTimer timer;
+    auto       enqueue = [&](cudaStream_t s2, StageTimer* tm) {
+        if (count)
+            enqueue_wave<kStack, true>(w.args, max_depth, ls, s2, tm);
+        else
+            enqueue_wave<kStack, false>(w.args, max_depth, ls, s2, tm);
+    };
+    if (p0.use_graph && !stages)
     {
         cudaGraph_t     graph;
         cudaGraphExec_t exec;
         cudaStream_t    cap;
         CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
         CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        enqueue_wave<kStack>(w.args, max_depth, ls, cap);
+        enqueue(cap, nullptr);
         CK(cudaStreamEndCapture(cap, &graph));
         CK(cudaGraphInstantiate(&exec, graph, 0));
         for (int64_t k = 0; k < num_chunks; ++k)
@@ -948,7 +1054,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     {
         for (int64_t k = 0; k < num_chunks; ++k)
         {
-            enqueue_wave<kStack>(w.args, max_depth, ls, st);
+            enqueue(st, stages ? &timer : nullptr);
             launches += 3 + 3 * (max_depth + 1);
         }
         CK(cudaGetLastError());
@@ -960,7 +1066,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
             CK(cudaMemcpyAsync(outs[j], dev_images[j], sizeof(float) * 3 * cams[j].width * cams[j].height,
                                cudaMemcpyDeviceToHost, st));
     }
-    unsigned long long hstats[4];
+    unsigned long long hstats[8];
     int                herr = 0;
     CK(cudaMemcpyAsync(hstats, w.stats, sizeof(hstats), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&herr, w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -969,6 +1075,8 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    float stage_ms[4] = {0.f, 0.f, 0.f, 0.f};
+    timer.sum(stage_ms);
     cleanup();
     if (stats)
     {
@@ -978,6 +1086,17 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
         stats->waves = static_cast<int32_t>(num_chunks);
         stats->kernel_launches = launches;
         stats->device_ms = ms;
+        for (int k = 0; k < 4; ++k) stats->stage_ms[k] = stage_ms[k];
+        stats->extend_launches = static_cast<int32_t>(num_chunks * (max_depth + 1));
+        stats->ext_nodes = static_cast<int64_t>(hstats[2]);
+        stats->ext_tris = static_cast<int64_t>(hstats[3]);
+        stats->nee_nodes = static_cast<int64_t>(hstats[4]);
+        stats->nee_tris = static_cast<int64_t>(hstats[5]);
+        int64_t img_bytes = 0;
+        for (int j = 0; j < num_jobs; ++j) img_bytes += 12 * static_cast<int64_t>(cams[j].width) * cams[j].height;
+        stats->h2d_bytes = static_cast<int64_t>(sizeof(JobGPU)) * num_jobs + 8 * static_cast<int64_t>(table.size());
+        stats->d2h_bytes = static_cast<int64_t>(sizeof(hstats) + sizeof(herr)) +
+                           (ptr_mode != MCRT_PTR_DEVICE ? img_bytes : 0);
     }
     if (herr & kErrStack) return fail(MCRT_ERR_STACK_OVERFLOW, "traversal stack overflow");
     if (herr & kErrQueue) return fail(MCRT_ERR_QUEUE_OVERFLOW, "queue overflow");
@@ -1236,10 +1355,130 @@ int mcrt_render_batch(int32_t n, mcrt_scene* const* scenes, const mcrt_camera* c
     }
 }
 
-int mcrt_render_adjoint(mcrt_scene*, const mcrt_camera*, const mcrt_render_params*, const float*, float*, int32_t,
-                        float*, int32_t, mcrt_render_stats*, void*)
+int mcrt_render_adjoint(mcrt_scene* s, const mcrt_camera* c, const mcrt_render_params* p, const float* dL,
+                        float* d_albedo, int32_t n_albedo, float* d_emis, int32_t n_emis, mcrt_render_stats* stats,
+                        void* stream)
 {
-    return fail(MCRT_ERR_INTERNAL, "adjoint not built yet");
+    try
+    {
+        int rc = validate_job(s, c, p);
+        if (rc) return rc;
+        if (!dL || (n_albedo > 0 && !d_albedo) || (n_emis > 0 && !d_emis) || n_albedo < 0 || n_emis < 0)
+            return fail(MCRT_ERR_INVALID_ARGUMENT, "null gradient or dL/dimage buffer");
+        if (s->bvh_depth + 2 >= kStack) return fail(MCRT_ERR_STACK_OVERFLOW, "BVH deeper than the traversal stack");
+        std::lock_guard<std::mutex> lock(s->mu);
+        CK(cudaSetDevice(s->device));
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        int64_t      px = static_cast<int64_t>(c->width) * c->height;
+        const float* d_dl = dL;
+        float*       dga = d_albedo;
+        float*       dge = d_emis;
+        std::vector<void*> temp;
+        auto cleanup = [&]() {
+            for (void* t : temp) cudaFree(t);
+        };
+        auto dev_alloc = [&](size_t bytes) -> void* {
+            void* d = nullptr;
+            if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+            temp.push_back(d);
+            return d;
+        };
+        if (p->ptr_mode != MCRT_PTR_DEVICE)
+        {
+            void* a1 = dev_alloc(sizeof(float) * 3 * px);
+            void* a2 = dev_alloc(sizeof(float) * 3 * std::max(n_albedo, 1));
+            void* a3 = dev_alloc(sizeof(float) * 3 * std::max(n_emis, 1));
+            if (!a1 || !a2 || !a3)
+            {
+                cleanup();
+                return fail(MCRT_ERR_OUT_OF_MEMORY, "adjoint buffer allocation failed");
+            }
+            CK(cudaMemcpyAsync(a1, dL, sizeof(float) * 3 * px, cudaMemcpyHostToDevice, st));
+            if (n_albedo > 0)
+                CK(cudaMemcpyAsync(a2, d_albedo, sizeof(float) * 3 * n_albedo, cudaMemcpyHostToDevice, st));
+            if (n_emis > 0) CK(cudaMemcpyAsync(a3, d_emis, sizeof(float) * 3 * n_emis, cudaMemcpyHostToDevice, st));
+            d_dl = static_cast<const float*>(a1);
+            dga = static_cast<float*>(a2);
+            dge = static_cast<float*>(a3);
+        }
+        Workspace& w = s->ws;
+        rc = ensure_workspace(w, 64, 1, 1);
+        if (rc)
+        {
+            cleanup();
+            return rc;
+        }
+        CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
+        CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
+        AdjointArgs aa;
+        aa.job.scene = s->view;
+        aa.job.cam = make_camera(*c);
+        aa.job.width = c->width;
+        aa.job.height = c->height;
+        aa.job.spp = p->spp;
+        aa.job.max_depth = p->max_depth;
+        aa.job.rr_depth = p->rr_depth;
+        aa.job.traverse = p->traverse;
+        aa.job.seed = p->seed;
+        aa.job.path_offset = 0;
+        aa.job.image = nullptr;
+        aa.dLdI = d_dl;
+        aa.g_albedo = dga;
+        aa.n_albedo = n_albedo;
+        aa.g_emis = dge;
+        aa.n_emis = n_emis;
+        aa.total_paths = px * p->spp;
+        aa.stats = w.stats;
+        aa.err = w.err;
+        size_t gbytes = sizeof(float) * 3 * static_cast<size_t>(n_albedo + n_emis);
+        aa.shared_grads = gbytes <= 96 * 1024 ? 1 : 0;
+        size_t dyn = aa.shared_grads ? gbytes : 0;
+        if (dyn > 48 * 1024)
+            CK(cudaFuncSetAttribute(k_adjoint<kStack>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(dyn)));
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint<kStack>, kAdjBlock, dyn);
+        int64_t want = (aa.total_paths + kAdjBlock - 1) / kAdjBlock;
+        int     grid = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(num_sms()) * std::max(occ, 1)));
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        CK(cudaEventRecord(e0, st));
+        k_adjoint<kStack><<<grid, kAdjBlock, dyn, st>>>(aa);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(e1, st));
+        if (p->ptr_mode != MCRT_PTR_DEVICE)
+        {
+            if (n_albedo > 0)
+                CK(cudaMemcpyAsync(d_albedo, dga, sizeof(float) * 3 * n_albedo, cudaMemcpyDeviceToHost, st));
+            if (n_emis > 0) CK(cudaMemcpyAsync(d_emis, dge, sizeof(float) * 3 * n_emis, cudaMemcpyDeviceToHost, st));
+        }
+        unsigned long long hstats[4];
+        int                herr = 0;
+        CK(cudaMemcpyAsync(hstats, w.stats, sizeof(hstats), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&herr, w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cleanup();
+        if (stats)
+        {
+            stats->paths = aa.total_paths;
+            stats->extension_rays = static_cast<int64_t>(hstats[0]);
+            stats->shadow_rays = 0;
+            stats->waves = 1;
+            stats->kernel_launches = 1;
+            stats->device_ms = ms;
+        }
+        if (herr & kErrStack) return fail(MCRT_ERR_STACK_OVERFLOW, "traversal stack overflow");
+        return MCRT_OK;
+    }
+    catch (...)
+    {
+        return fail(MCRT_ERR_INTERNAL, "unexpected exception in mcrt_render_adjoint");
+    }
 }
 
 }  // extern "C"

@@ -1,0 +1,118 @@
+// Drop-in SceneBVH backend for MCRT: the GB300 library behind the reference's own
+// scene/BVH seam (src/core/scenebvh.h:11-25).  Compile this file into MCRT's rtcore in
+// place of src/core/scenebvh.cpp and link libmcrt_gb300.so; Scene::intersect / occluded
+// (scene.cpp:77-85) and everything above them (rayTrace, lightPdfW, lightRadiance, ...)
+// then run their ray queries on the GPU, unchanged.
+//
+// Semantics kept from the reference backend (scenebvh.cpp:340-445):
+//   * SceneBVH keeps a reference to the caller's triangle vector, which must outlive it;
+//   * intersect(): tmin = NUM_EPS_RAY, tmax = infinity, HitInfo carries t, u, v, the
+//     interpolated shading normal, the primitive id and the material id;
+//   * occluded(ray, tfar): a hit with NUM_EPS_RAY < t < tfar - NUM_EPS_RAY;
+//   * hits are bit-identical to the SplitBVH backend when the reference tree is passed in
+//     (MCRT_BUILD_EXTERNAL + MCRT_TRAVERSE_REF); with the library's own tree and the
+//     watertight traversal (the defaults below) they agree on every non-marginal ray.
+// The reference has no error channel; a failed call prints mcrt_last_error() and aborts,
+// as the reference's builder does on its own failures (splitbvh.cpp:1556, 1596).
+//
+// One call per ray is correct but launch-bound; for throughput call mcrt_trace_closest /
+// mcrt_trace_any on batches, or replace DemoSimple::run with mcrt_render.
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "constants.h"
+#include "intersection.h"
+#include "mcrt_gb300.h"
+#include "ray.h"
+#include "scenebvh.h"
+#include "triangle.h"
+
+namespace {
+
+struct Gb300Context
+{
+    mcrt_scene* scene = nullptr;
+};
+
+void check(int rc, const char* what)
+{
+    if (rc != MCRT_OK)
+    {
+        std::fprintf(stderr, "%s failed (%d): %s\n", what, rc, mcrt_last_error());
+        std::abort();
+    }
+}
+
+}  // namespace
+
+SceneBVH::SceneBVH(const std::vector<TriangleObject>& triangles) : m_triangles_ref(triangles)
+{
+    const size_t         n = triangles.size();
+    std::vector<float>   verts(9 * n), normals(9 * n);
+    std::vector<int32_t> mat_ids(n, 0);
+    for (size_t i = 0; i < n; ++i)
+    {
+        const TriangleObject& t = triangles[i];
+        const vec3*           v[6] = {&t.a, &t.b, &t.c, &t.na, &t.nb, &t.nc};
+        for (int k = 0; k < 3; ++k)
+        {
+            verts[9 * i + 3 * k + 0] = v[k]->x;
+            verts[9 * i + 3 * k + 1] = v[k]->y;
+            verts[9 * i + 3 * k + 2] = v[k]->z;
+            normals[9 * i + 3 * k + 0] = v[3 + k]->x;
+            normals[9 * i + 3 * k + 1] = v[3 + k]->y;
+            normals[9 * i + 3 * k + 2] = v[3 + k]->z;
+        }
+    }
+    // the backend only answers ray queries; shading stays in MCRT, so one material suffices
+    mcrt_material m = {MCRT_MAT_DIFF, {1.f, 1.f, 1.f}, 1.f, 1.33f, -1, -1};
+    mcrt_scene_desc d = {};
+    d.num_triangles = static_cast<int64_t>(n);
+    d.vertices = verts.data();
+    d.normals = normals.data();
+    d.material_ids = mat_ids.data();
+    d.num_materials = 1;
+    d.materials = &m;
+    d.builder = MCRT_BUILD_SAH;
+    Gb300Context* ctx = new Gb300Context;
+    check(mcrt_scene_create(&d, &ctx->scene), "mcrt_scene_create");
+    m_ctx = ctx;
+}
+
+SceneBVH::~SceneBVH()
+{
+    Gb300Context* ctx = static_cast<Gb300Context*>(m_ctx);
+    if (ctx) mcrt_scene_destroy(ctx->scene);
+    delete ctx;
+}
+
+HitInfo SceneBVH::intersect(const Ray& ray) const
+{
+    Gb300Context* ctx = static_cast<Gb300Context*>(m_ctx);
+    mcrt_ray      r = {{ray.orig.x, ray.orig.y, ray.orig.z}, NUM_EPS_RAY, {ray.dir.x, ray.dir.y, ray.dir.z},
+                       NUM_INFINITY};
+    mcrt_hit      h;
+    check(mcrt_trace_closest(ctx->scene, &r, 1, &h, MCRT_TRAVERSE_FAST, MCRT_PTR_HOST, nullptr), "mcrt_trace_closest");
+    if (h.prim < 0)
+    {
+        HitInfo miss;
+        miss.reset();
+        return miss;
+    }
+    const TriangleObject& tri = m_triangles_ref[h.prim];
+    HitInfo               isect(h.t, h.u, h.v, tri.normal(h.u, h.v), &tri);
+    isect.setPrimitiveID(h.prim);
+    isect.setMaterialID(tri.materialID());
+    return isect;
+}
+
+bool SceneBVH::occluded(const Ray& ray, float tfar) const
+{
+    Gb300Context* ctx = static_cast<Gb300Context*>(m_ctx);
+    mcrt_ray      r = {{ray.orig.x, ray.orig.y, ray.orig.z}, NUM_EPS_RAY, {ray.dir.x, ray.dir.y, ray.dir.z},
+                       tfar - NUM_EPS_RAY};
+    int32_t       occ = 0;
+    check(mcrt_trace_any(ctx->scene, &r, 1, &occ, MCRT_TRAVERSE_FAST, MCRT_PTR_HOST, nullptr), "mcrt_trace_any");
+    return occ != 0;
+}

@@ -199,9 +199,10 @@ class GpuScene:
 
     # -- rayTrace + DemoSimple::run -----------------------------------------------------
     def render(self, camera: CameraDesc, spp: int, max_depth: int, rr_depth: int = -1, seed: int = 0,
-               traverse: int = N.TRAVERSE_FAST, out=None, path_chunk: int = 0, use_graph: bool = False):
+               traverse: int = N.TRAVERSE_FAST, out=None, path_chunk: int = 0, use_graph: bool = False,
+               profile: int = 0):
         """Returns (image (H, W, 3) float32, stats dict).  `out` may be a CUDA tensor."""
-        p = make_params(spp, max_depth, rr_depth, seed, traverse, path_chunk, use_graph)
+        p = make_params(spp, max_depth, rr_depth, seed, traverse, path_chunk, use_graph, profile)
         cam = camera.to_c()
         st = N.RenderStats()
         if out is not None and _is_torch(out):
@@ -252,7 +253,8 @@ class GpuScene:
                 "mcrt_scene_set_materials")
 
 
-def make_params(spp, max_depth, rr_depth=-1, seed=0, traverse=N.TRAVERSE_FAST, path_chunk=0, use_graph=False):
+def make_params(spp, max_depth, rr_depth=-1, seed=0, traverse=N.TRAVERSE_FAST, path_chunk=0, use_graph=False,
+                profile=0):
     p = N.RenderParams()
     p.spp = int(spp)
     p.max_depth = int(max_depth)
@@ -261,13 +263,16 @@ def make_params(spp, max_depth, rr_depth=-1, seed=0, traverse=N.TRAVERSE_FAST, p
     p.traverse = int(traverse)
     p.path_chunk = int(path_chunk)
     p.use_graph = 1 if use_graph else 0
+    p.profile = int(profile)
     return p
 
 
 def stats_dict(st: N.RenderStats) -> dict:
     return {"paths": st.paths, "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
             "rays": st.extension_rays + st.shadow_rays, "waves": st.waves, "kernel_launches": st.kernel_launches,
-            "device_ms": st.device_ms}
+            "device_ms": st.device_ms, "stage_ms": list(st.stage_ms), "extend_launches": st.extend_launches,
+            "ext_nodes": st.ext_nodes, "ext_tris": st.ext_tris, "nee_nodes": st.nee_nodes, "nee_tris": st.nee_tris,
+            "h2d_bytes": st.h2d_bytes, "d2h_bytes": st.d2h_bytes}
 
 
 def render_batch(scenes: list, cameras: list, params: list, outs: list | None = None):

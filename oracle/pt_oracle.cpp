@@ -833,8 +833,8 @@ struct Scene
         }
     }
 
-    // conservative slab test (bounds widened by a few ulp, Ize 2013)
-    static bool boxHit(const Node& nd, const V3<T>& o, const V3<T>& inv, T tmin, T tmax)
+    // conservative slab test (bounds widened by a few ulp, Ize 2013); entry distance in tnear
+    static bool boxHit(const Node& nd, const V3<T>& o, const V3<T>& inv, T tmin, T tmax, T* tnear = nullptr)
     {
         T t0 = tmin, t1 = tmax;
         for (int k = 0; k < 3; ++k)
@@ -849,6 +849,7 @@ struct Scene
             t1 = hi < t1 ? hi : t1;
             if (t0 > t1) return false;
         }
+        if (tnear) *tnear = t0;
         return true;
     }
 
@@ -888,8 +889,27 @@ struct Scene
             }
             else
             {
-                stack[sp++] = nd.right;
-                stack[sp++] = nd.left;
+                // front-to-back: push the farther child first (results do not depend on it)
+                T    tl = 0, tr = 0;
+                bool hl = boxHit(nodes[nd.left], o, inv, tmin, best, &tl);
+                bool hr = boxHit(nodes[nd.right], o, inv, tmin, best, &tr);
+                if (hl && hr)
+                {
+                    if (tl <= tr)
+                    {
+                        stack[sp++] = nd.right;
+                        stack[sp++] = nd.left;
+                    }
+                    else
+                    {
+                        stack[sp++] = nd.left;
+                        stack[sp++] = nd.right;
+                    }
+                }
+                else if (hl)
+                    stack[sp++] = nd.left;
+                else if (hr)
+                    stack[sp++] = nd.right;
             }
         }
         return h;

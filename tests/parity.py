@@ -8,8 +8,10 @@ Hit parity (closest hit of the same rays on the same triangles):
     within 4 ulp on every non-marginal ray.  A disagreement is marginal when, for
     either of the two triangles involved, |det_MT| lies within 2^-8 of the 1e-6
     rejection threshold, a barycentric coordinate is within 2^-20 of an edge, the
-    two hits lie within 4 ulp of each other (a tie), or the ray has a zero
-    direction component (the reference's inv_dir = 0 slab test, ray.cpp:39-42).
+    ray origin lies within 8 ulp (of its largest coordinate) of the triangle's plane
+    (a self-intersection, where t is rounding noise), the two hits lie within 4 ulp
+    of each other (a tie), or the ray has a zero direction component (the
+    reference's inv_dir = 0 slab test, ray.cpp:39-42).
 """
 from __future__ import annotations
 
@@ -58,20 +60,26 @@ def mt_terms(verts: np.ndarray, prim: np.ndarray, rays: np.ndarray):
     return np.abs(det), bmin, t
 
 
+def plane_distance(verts, prim, rays):
+    tri = verts.reshape(-1, 3, 3)[np.maximum(prim, 0)].astype(np.float64)
+    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-300)
+    return np.abs(np.sum((rays[:, 0:3].astype(np.float64) - tri[:, 0]) * n, axis=1))
+
+
 def classify(verts, rays, ref_t, ref_p, got_t, got_p):
-    """Returns (mismatch_unexplained mask, marginal mask)."""
+    """Returns (unexplained disagreement mask, marginal disagreement mask)."""
     same = (ref_p == got_p) & ((ref_p < 0) | (ulp_diff(ref_t, got_t) <= 4))
     marginal = np.zeros(rays.shape[0], bool)
-    zero_dir = np.any(rays[:, 4:7] == 0.0, axis=1)
-    marginal |= zero_dir
+    marginal |= np.any(rays[:, 4:7] == 0.0, axis=1)
     lo, hi = 1e-6 * (1 - 2.0 ** -8), 1e-6 * (1 + 2.0 ** -8)
+    oulp = np.spacing(np.max(np.abs(rays[:, 0:3]), axis=1).astype(np.float32)).astype(np.float64)
     for p in (ref_p, got_p):
         det, bmin, _ = mt_terms(verts, p, rays)
         m = (p >= 0) & (((det >= lo) & (det <= hi)) | (np.abs(bmin) < 2.0 ** -20))
+        m |= (p >= 0) & (plane_distance(verts, p, rays) <= 8 * oulp)
         marginal |= m
     both = (ref_p >= 0) & (got_p >= 0)
     marginal |= both & (ulp_diff(ref_t, got_t) <= 4)
-    # a hit lost or gained on a triangle whose |det| is near the cull threshold, or a
-    # grazing edge: check the triangle the other side reported as well
     bad = ~same & ~marginal
-    return bad, marginal
+    return bad, marginal & ~same

@@ -1,0 +1,95 @@
+"""The path-replay adjoint: against the FP64 CPU adjoint of the oracle (same seeds) and
+against central finite differences with common random numbers (step 1e-3)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RES, SPP, DEPTH = 32, 16, 6
+
+
+def _setup(seed=3):
+    from mcrt_gb300 import GpuScene, scenes
+    desc, albedo, emission = scenes.cfg3_scene(param_seed=seed)
+    cam = scenes.cfg0_camera(RES, RES)
+    return desc, cam, albedo, emission, GpuScene(desc)
+
+
+def _loss_and_grad_image(img, target):
+    d = img - target
+    return float(np.sum(d.astype(np.float64) ** 2)), (2.0 * d).astype(np.float32)
+
+
+def test_adjoint_matches_fp64_oracle_adjoint(cuda_device):
+    from oracle.oracle import OracleScene
+    desc, cam, albedo, emission, sc = _setup()
+    rng = np.random.default_rng(0)
+    dl = rng.normal(size=(RES, RES, 3)).astype(np.float32)
+    ga, ge, st = sc.render_adjoint(cam, SPP, DEPTH, dl, albedo.shape[0], 1, seed=11)
+    ref = OracleScene(desc, 64).render(cam.as_array(), RES, RES, SPP, DEPTH, -1, seed=11, dLdI=dl,
+                                       n_albedo=albedo.shape[0], n_emission=1)
+    for got, want, name in ((ga, ref["g_albedo"], "albedo"), (ge, ref["g_emission"], "emission")):
+        err = np.linalg.norm(got - want) / np.linalg.norm(want)
+        assert err < 2e-2, f"{name}: relative L2 error {err:.3e}"
+    assert st["paths"] == RES * RES * SPP
+
+
+def test_adjoint_vs_central_finite_differences(cuda_device):
+    """Directional derivatives of an L2 image loss: adjoint vs (L(p + h v) - L(p - h v)) / 2h."""
+    desc, cam, albedo, emission, sc = _setup()
+    from mcrt_gb300 import scenes
+    target_desc, _, _ = scenes.cfg3_scene(param_seed=99)
+    from mcrt_gb300 import GpuScene
+    target, _ = GpuScene(target_desc).render(cam, spp=SPP, max_depth=DEPTH, seed=5)
+
+    def loss_at(a, e):
+        sc.set_materials(scenes.cfg3_with_params(a, e).materials)
+        img, _ = sc.render(cam, spp=SPP, max_depth=DEPTH, seed=11)
+        return _loss_and_grad_image(img, target)
+
+    L0, dl = loss_at(albedo, emission)
+    ga, ge, _ = sc.render_adjoint(cam, SPP, DEPTH, dl, albedo.shape[0], 1, seed=11)
+    rng = np.random.default_rng(1)
+    h = 1e-3
+    for trial in range(3):
+        va = rng.normal(size=albedo.shape).astype(np.float32)
+        ve = rng.normal(size=emission.shape).astype(np.float32) * (0.0 if trial < 2 else 1.0)
+        Lp, _ = loss_at(albedo + h * va, emission + h * ve)
+        Lm, _ = loss_at(albedo - h * va, emission - h * ve)
+        fd = (Lp - Lm) / (2 * h)
+        an = float(np.sum(ga * va) + np.sum(ge * ve))
+        assert abs(an - fd) <= 0.02 * abs(fd) + 1e-6, f"trial {trial}: adjoint {an:.6g} vs FD {fd:.6g}"
+    sc.set_materials(scenes.cfg3_with_params(albedo, emission).materials)
+
+
+def test_torch_autograd_function(cuda_device):
+    import torch
+    from mcrt_gb300.autograd import DiffRender
+    desc, cam, albedo, emission, sc = _setup()
+    r = DiffRender(sc, cam, spp=8, max_depth=DEPTH, seed=2)
+    a = torch.tensor(albedo, device=cuda_device, requires_grad=True)
+    e = torch.tensor(emission, device=cuda_device, requires_grad=True)
+    img = r(a, e)
+    w = torch.randn_like(img)
+    (img * w).sum().backward()
+    ga, ge, _ = sc.render_adjoint(cam, 8, DEPTH, w, albedo.shape[0], 1, seed=2)
+    np.testing.assert_allclose(a.grad.cpu().numpy(), ga.cpu().numpy(), rtol=1e-4, atol=1e-6)
+    np.testing.assert_allclose(e.grad.cpu().numpy(), ge.cpu().numpy(), rtol=1e-4, atol=1e-6)
+
+
+def test_adjoint_forward_time_ratio(cuda_device):
+    """Forward + adjoint stays within 3x the forward time (same image, same spp)."""
+    import time
+    desc, cam, albedo, emission, sc = _setup()
+    from mcrt_gb300 import scenes
+    big = scenes.cfg0_camera(128, 128)
+    dl = np.ones((128, 128, 3), np.float32)
+    sc.render(big, spp=SPP, max_depth=DEPTH, seed=1)
+    t0 = time.perf_counter()
+    _, fst = sc.render(big, spp=SPP, max_depth=DEPTH, seed=1)
+    tf = time.perf_counter() - t0
+    sc.render_adjoint(big, SPP, DEPTH, dl, albedo.shape[0], 1, seed=1)
+    t0 = time.perf_counter()
+    sc.render_adjoint(big, SPP, DEPTH, dl, albedo.shape[0], 1, seed=1)
+    ta = time.perf_counter() - t0
+    assert (tf + ta) / tf <= 3.0, f"forward {tf * 1e3:.1f} ms, adjoint {ta * 1e3:.1f} ms"

@@ -83,3 +83,22 @@ def test_struct_layouts_match_header(tmp_path):
         assert int(got[cname]) == ctypes.sizeof(py), cname
         for fname, _ in py._fields_:
             assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, f"{cname}.{fname}"
+
+
+def test_scenebvh_adapter_compiles_against_reference_headers(tmp_path):
+    """The drop-in SceneBVH backend compiles against the reference's own headers and
+    links against the library (where the reference sources are present)."""
+    import subprocess
+    import pytest
+    ref = os.environ.get("MCRT_REFERENCE_DIR", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "src", "core")):
+        pytest.skip("reference sources not present on this machine")
+    src = os.path.join(ROOT, "mcrt_gb300", "integration", "scenebvh_gb300.cpp")
+    obj = tmp_path / "scenebvh_gb300.o"
+    subprocess.run(["g++", "-std=c++11", "-c", "-fPIC", src, "-o", str(obj), f"-I{ref}/src/core",
+                    f"-I{ref}/src/thirdparty/glm/include", f"-I{ref}/src/thirdparty/nanolog",
+                    f"-I{os.path.join(ROOT, 'include')}"], check=True)
+    out = subprocess.run(["nm", "-C", str(obj)], capture_output=True, text=True, check=True).stdout
+    for sym in ("SceneBVH::SceneBVH", "SceneBVH::intersect", "SceneBVH::occluded", "SceneBVH::~SceneBVH"):
+        assert sym in out
+    assert "U mcrt_trace_closest" in out and "U mcrt_scene_create" in out

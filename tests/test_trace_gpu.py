@@ -72,8 +72,8 @@ def test_fast_mode_nonmarginal(name, builder, cuda_device):
         total += rays.shape[0]
         if k != "axis":
             marginal_total += int(marginal.sum())
-    # the marginal class stays small apart from the zero-direction rays
-    assert marginal_total <= max(8, total // 200)
+    # marginal disagreements stay rare apart from the zero-direction rays
+    assert marginal_total <= max(8, total // 200), f"{marginal_total} marginal disagreements of {total}"
 
 
 @pytest.mark.parametrize("builder", ["external", "sah"])
