@@ -209,7 +209,7 @@ def main():
     for w in range(args.warmup):
         sc.render(cam, seed=100 + w, out=out, profile=PROFILE_STAGES, **kw)
     # timed region: one render per step, stage events inside, L2 flushed between steps
-    step_ms, rays, paths, extend_ms, extend_launches = [], 0, 0, 0.0, 0
+    step_ms, rays, paths, extend_ms, connect_ms, extend_launches = [], 0, 0, 0.0, 0.0, 0
     st_last = None
     with ClockSampler(local) as clk:
         for k in range(args.steps):
@@ -225,6 +225,7 @@ def main():
             rays += st["rays"]
             paths += st["paths"]
             extend_ms += st["stage_ms"][1]
+            connect_ms += st["stage_ms"][3]
             extend_launches += st["extend_launches"]
             st_last = st
     clocks = clk.summary()
@@ -239,13 +240,29 @@ def main():
     value = rays / (total_ms / 1e3) / 1e6
     msamples = paths / (total_ms / 1e3) / 1e6
 
-    # algorithmic bytes of the extension traversal: a counting render of the same seeds
+    # algorithmic bytes of the two traversal kernels: a counting render of the same seeds.
+    # k_extend per extension ray: 64 B per node, 48 B per triangle tested, 32 B ray + 16 B hit;
+    # k_connect per next-event ray: nodes/triangles as above, 64 B ray + payload + meta in,
+    # 16 B result out.  Both kernels launch once per depth per wave.
     _, sc_cnt = sc.render(cam, seed=0, out=out, profile=PROFILE_COUNT, **kw)
     ext_bytes = 64 * sc_cnt["ext_nodes"] + 48 * sc_cnt["ext_tris"] + (32 + 16) * sc_cnt["extension_rays"]
-    per_launch_bytes = ext_bytes / max(st_last["extend_launches"], 1)
-    avg_launch_ms = extend_ms / max(extend_launches, 1)
+    nee_bytes = 64 * sc_cnt["nee_nodes"] + 48 * sc_cnt["nee_tris"] + (64 + 16) * sc_cnt["shadow_rays"]
+    launches_per_render = max(st_last["extend_launches"], 1)
+    kernels = {
+        "k_extend (closest-hit traversal of extension rays)": (ext_bytes, extend_ms, sc_cnt["extension_rays"],
+                                                                sc_cnt["ext_nodes"], sc_cnt["ext_tris"]),
+        "k_connect (next-event rays: any-hit / bounded closest-hit)": (nee_bytes, connect_ms, sc_cnt["shadow_rays"],
+                                                                        sc_cnt["nee_nodes"], sc_cnt["nee_tris"]),
+    }
+    dom = max(kernels, key=lambda k: kernels[k][1])
+    bytes_per_render, kern_ms, kern_rays, kern_nodes, kern_tris = kernels[dom]
+    per_launch_bytes = bytes_per_render / launches_per_render
+    avg_launch_ms = kern_ms / max(extend_launches, 1)
     achieved = per_launch_bytes / (avg_launch_ms / 1e3) / 1e9 if avg_launch_ms > 0 else 0.0
     peak, peak_kind = measured_peak_hbm()
+    other = [k for k in kernels if k != dom][0]
+    ob, oms = kernels[other][0], kernels[other][1]
+    other_achieved = (ob / launches_per_render) / (oms / max(extend_launches, 1) / 1e3) / 1e9 if oms > 0 else 0.0
 
     # e2e: the C-ABI call with host buffers (image copied back inside the call)
     host_img = np.zeros((cam.height, cam.width, 3), np.float32)
@@ -265,7 +282,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rows = {"cfg0": (96, 160), "cfg1": (448, 480)}[args.workload]
+        rows = {"cfg0": (64, 192), "cfg1": (384, 640)}[args.workload]
         c_rays, c_paths, c_dt, c_build = cpu_port_sample(desc, cam, p, rows)
         cpu = {"value": round(c_rays / c_dt / 1e6, 3), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                "sample": f"{args.workload} rows {rows[0]}-{rows[1]} x {cam.width} px x {p['spp']} spp "
@@ -281,14 +298,19 @@ def main():
                        "scene_setup_s": round(setup_s, 2)},
             "msamples_per_s": round(msamples, 3),
             "rays_per_path": round(rays / max(paths, 1), 3),
-            "roofline": {"bound": "hbm", "kernel": "k_extend (closest-hit traversal)", "achieved": round(achieved, 1),
-                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
                          "peak_source": peak_kind,
-                         "bytes_per_ray": round(ext_bytes / max(sc_cnt["extension_rays"], 1), 1),
-                         "nodes_per_ray": round(sc_cnt["ext_nodes"] / max(sc_cnt["extension_rays"], 1), 2),
-                         "tris_per_ray": round(sc_cnt["ext_tris"] / max(sc_cnt["extension_rays"], 1), 2),
-                         "extend_share_of_step": round(extend_ms / max(total_ms, 1e-9), 3)},
-            "stage_ms_per_step": [round(x, 2) for x in st_last["stage_ms"]],
+                         "bytes_per_ray": round(bytes_per_render / max(kern_rays, 1), 1),
+                         "nodes_per_ray": round(kern_nodes / max(kern_rays, 1), 2),
+                         "tris_per_ray": round(kern_tris / max(kern_rays, 1), 2),
+                         "share_of_step": round(kern_ms / max(total_ms, 1e-9), 3),
+                         "second_kernel": {"kernel": other, "achieved": round(other_achieved, 1),
+                                           "frac": round(other_achieved / peak, 4),
+                                           "share_of_step": round(oms / max(total_ms, 1e-9), 3)}},
+            "stage_ms_per_step": {"raygen+resolve": round(st_last["stage_ms"][0], 2),
+                                  "extend": round(st_last["stage_ms"][1], 2), "shade": round(st_last["stage_ms"][2], 2),
+                                  "connect": round(st_last["stage_ms"][3], 2)},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},

@@ -15,6 +15,7 @@
  *   SceneBVH::~SceneBVH           src/core/scenebvh.cpp:398-402                -> mcrt_scene_destroy
  *   rayTrace + DemoSimple::run    src/examples/pt/demo_pt.cpp:512-720        -> mcrt_render
  *   (no reference counterpart: path-replay adjoint, batched launch)           -> mcrt_render_adjoint,
+ *                                                                                mcrt_render_adjoint_batch,
  *                                                                                mcrt_render_batch
  */
 #ifndef MCRT_GB300_H
@@ -151,7 +152,7 @@ typedef struct mcrt_render_stats {
     int32_t waves;
     int32_t kernel_launches;
     float   device_ms;   /* CUDA-event time of the kernels (excludes host copies) */
-    float   stage_ms[4]; /* MCRT_PROFILE_STAGES: begin+raygen, extend, shade, connect+resolve */
+    float   stage_ms[4]; /* MCRT_PROFILE_STAGES: begin+raygen+resolve, extend, shade, connect */
     int32_t extend_launches;
     int64_t ext_nodes;   /* MCRT_PROFILE_COUNT: nodes fetched / triangles tested by extension */
     int64_t ext_tris;    /* rays, and by next-event rays */
@@ -196,11 +197,20 @@ int mcrt_render_adjoint(mcrt_scene* scene, const mcrt_camera* camera, const mcrt
                         const float* dL_dimage, float* d_albedo, int32_t num_albedo_params, float* d_emission,
                         int32_t num_emission_params, mcrt_render_stats* stats, void* stream);
 
+/* The adjoint of mcrt_render_batch: every job's paths replayed in one launch, gradients
+ * of all jobs summed into the same parameter vectors (e.g. many views of one scene).
+ * dL_dimages[j] is job j's dL/dimage; ADDS into d_albedo / d_emission. */
+int mcrt_render_adjoint_batch(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cameras,
+                              const mcrt_render_params* params, const float* const* dL_dimages, float* d_albedo,
+                              int32_t num_albedo_params, float* d_emission, int32_t num_emission_params,
+                              mcrt_render_stats* stats, void* stream);
+
 /* Many (scene, camera, params) jobs of uneven size in one wavefront: jobs share every
  * stage launch.  rgb_out[j] receives job j's image. */
 int mcrt_render_batch(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cameras,
                       const mcrt_render_params* params, float* const* rgb_out, mcrt_render_stats* stats,
                       void* stream);
+
 
 #ifdef __cplusplus
 }

@@ -5,6 +5,7 @@ Public surface:
   GpuScene                             device scene: trace_closest / trace_any / render /
                                        render_adjoint / set_materials
   render_batch                         many scenes/cameras/spp budgets in one wavefront
+  render_adjoint_batch                 the adjoint of render_batch in one launch
   build()                              compile the in-tree native library
 The native library (mcrt_gb300/_lib/libmcrt_gb300.so, C ABI in include/mcrt_gb300.h)
 is required: there is no CPU fallback.
@@ -13,8 +14,9 @@ from . import scenes
 from ._native import (PTR_DEVICE, PTR_HOST, TRAVERSE_FAST, TRAVERSE_REF, McrtError, load)
 from .native_build import build
 from .scene import (DIFF, GGX, GLSY, LGHT, REFR, SPEC, CameraDesc, GpuScene, Material, SceneDesc, make_params,
-                    render_batch)
+                    render_adjoint_batch, render_batch)
 
-__all__ = ["SceneDesc", "Material", "CameraDesc", "GpuScene", "render_batch", "build", "load", "scenes",
+__all__ = ["SceneDesc", "Material", "CameraDesc", "GpuScene", "render_batch", "render_adjoint_batch", "build", "load",
+           "scenes",
            "McrtError", "TRAVERSE_FAST", "TRAVERSE_REF", "PTR_HOST", "PTR_DEVICE", "make_params",
            "LGHT", "DIFF", "SPEC", "REFR", "GLSY", "GGX"]

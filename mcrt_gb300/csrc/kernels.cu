@@ -29,13 +29,11 @@
 #include "device.cuh"
 #include "estimator.cuh"
 #include "host.h"
+#include "wavefront.h"
 
 namespace mcrt {
 std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs);
 
-constexpr int kTraceBlock = 128;
-constexpr int kStack = 64;
-constexpr int kMaxDepth = 62;
 
 // ---------------------------------------------------------------------------
 // batch trace
@@ -63,42 +61,6 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(SceneView s, const float4
 // ---------------------------------------------------------------------------
 // wavefront state
 // ---------------------------------------------------------------------------
-struct Ctrl
-{
-    int64_t base;
-    int     count;
-    int     chunk;
-    int     qcount[kMaxDepth + 2];
-    int     scount[kMaxDepth + 1][2];
-};
-
-struct WaveArgs
-{
-    Ctrl*               ctrl;
-    const int64_t*      chunk_table;
-    const JobGPU*       jobs;
-    int                 num_jobs;
-    int64_t             capacity;
-    float4*             qo[2];
-    float4*             qd[2];
-    int*                qp[2];
-    float4*             hits;
-    float4*             thr;
-    float4*             rad;
-    uint64_t*           rng;
-    int*                pix;
-    int*                job;
-    float4*             nee_val;  // 4 next-event results per path slot (written by k_connect)
-    int*                pend;     // per path slot: mask of next-event results not yet added
-    float4*             so[2];  // [0] any-hit queue, [1] closest-hit queue
-    float4*             sd[2];
-    float4*             sv[2];
-    int4*               sm[2];
-    int64_t             shadow_cap;
-    unsigned long long* stats;  // [0] extension rays, [1] shadow rays, [2..5] work counters
-    int*                err;
-};
-
 // warp-reduced add of per-thread work counters into stats[slot], stats[slot + 1]
 __device__ __forceinline__ void flush_count(unsigned long long* stats, int slot, const TraceCount& c)
 {
@@ -400,8 +362,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_connect(WaveArgs a, int depth)
 // ---------------------------------------------------------------------------
 struct AdjointArgs
 {
-    JobGPU       job;
-    const float* dLdI;  // [H][W][3]
+    const JobGPU* jobs;  // per job: scene, camera, params; .image = dL/dimage [H][W][3]
+    int           num_jobs;
     float*       g_albedo;
     int          n_albedo;
     float*       g_emis;
@@ -427,14 +389,15 @@ __global__ void __launch_bounds__(kAdjBlock) k_adjoint(AdjointArgs a)
     __syncthreads();
     float* ga = a.shared_grads ? sgrad : a.g_albedo;
     float* ge = a.shared_grads ? sgrad + 3 * a.n_albedo : a.g_emis;
-    const JobGPU&    J = a.job;
-    const SceneView& S = J.scene;
     unsigned long long rays = 0;
     for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < a.total_paths;
          g += static_cast<int64_t>(gridDim.x) * blockDim.x)
     {
-        int pixel = static_cast<int>(g / J.spp);
-        int s = static_cast<int>(g - static_cast<int64_t>(pixel) * J.spp);
+        const JobGPU&    J = a.jobs[find_job(a.jobs, a.num_jobs, g)];
+        const SceneView& S = J.scene;
+        int64_t          local = g - J.path_offset;
+        int pixel = static_cast<int>(local / J.spp);
+        int s = static_cast<int>(local - static_cast<int64_t>(pixel) * J.spp);
         int x = pixel % J.width, y = pixel / J.width;
         Pcg rng;
         rng.seed(J.seed, static_cast<uint32_t>(pixel), static_cast<uint32_t>(s));
@@ -444,7 +407,8 @@ __global__ void __launch_bounds__(kAdjBlock) k_adjoint(AdjointArgs a)
         float3 o, d;
         camera_ray(J.cam, (static_cast<float>(x) + 0.5f + dx) / static_cast<float>(J.width),
                    (static_cast<float>(y) + 0.5f + dy) / static_cast<float>(J.height), o, d);
-        float3 dl = mk(a.dLdI[3 * pixel], a.dLdI[3 * pixel + 1], a.dLdI[3 * pixel + 2]) * (1.0f / J.spp);
+        const float* dLdI = J.image;
+        float3       dl = mk(dLdI[3 * pixel], dLdI[3 * pixel + 1], dLdI[3 * pixel + 2]) * (1.0f / J.spp);
         float3 L = mk(0.f, 0.f, 0.f), T = mk(1.f, 1.f, 1.f);
         bool   last_nee = false;
         // per-vertex log for the albedo adjoint
@@ -697,7 +661,7 @@ int num_sms()
     return sms;
 }
 
-CameraGPU make_camera(const mcrt_camera& c)
+CameraGPU make_camera_impl(const mcrt_camera& c)
 {
     // Camera::Camera (camera.cpp:9-35), in float with the same operation order
     auto sub = [](const float* a, const float* b, float* o) {
@@ -748,43 +712,8 @@ int ensure_workspace(Workspace& w, int64_t capacity, int num_jobs, int64_t num_c
     {
         cudaFree(w.block);
         w.block = nullptr;
-        int64_t C = capacity, S = 2 * capacity;
-        // per-path: qo,qd x2 (64 B), qp x2 (8), hits 16, thr 16, rad 16, rng 8, pix 4, job 4
-        // shadow: 2 queues x S x (so, sd, sv 48 B + sm 16 B)
-        size_t bytes = static_cast<size_t>(C) * (64 + 8 + 16 + 16 + 16 + 8 + 4 + 4 + 64 + 4) +
-                       static_cast<size_t>(S) * 2 * 64 + 64 * 32;
-        CK(cudaMalloc(&w.block, bytes));
-        char* p = static_cast<char*>(w.block);
-        auto take = [&](size_t n) {
-            size_t off = (reinterpret_cast<uintptr_t>(p) + 255) & ~static_cast<uintptr_t>(255);
-            char*  r = reinterpret_cast<char*>(off);
-            p = r + n;
-            return static_cast<void*>(r);
-        };
-        WaveArgs& a = w.args;
-        for (int k = 0; k < 2; ++k)
-        {
-            a.qo[k] = static_cast<float4*>(take(16 * C));
-            a.qd[k] = static_cast<float4*>(take(16 * C));
-            a.qp[k] = static_cast<int*>(take(4 * C));
-        }
-        a.hits = static_cast<float4*>(take(16 * C));
-        a.thr = static_cast<float4*>(take(16 * C));
-        a.rad = static_cast<float4*>(take(16 * C));
-        a.rng = static_cast<uint64_t*>(take(8 * C));
-        a.pix = static_cast<int*>(take(4 * C));
-        a.job = static_cast<int*>(take(4 * C));
-        a.nee_val = static_cast<float4*>(take(64 * C));
-        a.pend = static_cast<int*>(take(4 * C));
-        for (int k = 0; k < 2; ++k)
-        {
-            a.so[k] = static_cast<float4*>(take(16 * S));
-            a.sd[k] = static_cast<float4*>(take(16 * S));
-            a.sv[k] = static_cast<float4*>(take(16 * S));
-            a.sm[k] = static_cast<int4*>(take(16 * S));
-        }
-        a.capacity = C;
-        a.shadow_cap = S;
+        CK(cudaMalloc(&w.block, wave_bytes(capacity)));
+        carve_wave(w.args, w.block, capacity);
         w.capacity = capacity;
     }
     if (w.jobs_cap < num_jobs)
@@ -814,11 +743,6 @@ int ensure_workspace(Workspace& w, int64_t capacity, int num_jobs, int64_t num_c
     w.args.err = w.err;
     return MCRT_OK;
 }
-
-struct LaunchShape
-{
-    int grid_trace, grid_shade, grid_small, block;
-};
 
 // Stage events: one pair per stage launch when profiling (never inside a graph).
 struct StageTimer
@@ -872,12 +796,12 @@ void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaS
         k_connect<STACK, COUNT><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
         end();
     }
-    beg(3);
+    beg(0);
     k_resolve<<<ls.grid_small, 256, 0, st>>>(a);
     end();
 }
 
-int validate_job(const mcrt_scene* s, const mcrt_camera* c, const mcrt_render_params* p)
+int validate_job_impl(const mcrt_scene* s, const mcrt_camera* c, const mcrt_render_params* p)
 {
     if (!s || !c || !p) return fail(MCRT_ERR_INVALID_ARGUMENT, "null scene, camera or params");
     if (c->width <= 0 || c->height <= 0 || p->spp <= 0)
@@ -896,7 +820,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
 {
     for (int j = 0; j < num_jobs; ++j)
     {
-        int rc = validate_job(scenes[j], &cams[j], &params[j]);
+        int rc = validate_job_impl(scenes[j], &cams[j], &params[j]);
         if (rc) return rc;
         if (!outs[j]) return fail(MCRT_ERR_INVALID_ARGUMENT, "null image buffer");
     }
@@ -921,7 +845,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
         const mcrt_render_params& p = params[j];
         JobGPU&                   J = jobs[j];
         J.scene = scenes[j]->view;
-        J.cam = make_camera(c);
+        J.cam = make_camera_impl(c);
         J.width = c.width;
         J.height = c.height;
         J.spp = p.spp;
@@ -1005,15 +929,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
 
-    LaunchShape ls;
-    int         sms = num_sms();
-    int         occ_t = 0, occ_s = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend<kStack, false>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 128, 0);
-    ls.grid_trace = sms * std::max(occ_t, 1);
-    ls.grid_shade = sms * std::max(occ_s, 1);
-    ls.grid_small = sms * 8;
-    ls.block = 128;
+    LaunchShape ls = launch_shape();
 
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -1104,6 +1020,87 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
 }
 
 }  // namespace
+
+namespace mcrt {
+
+size_t wave_bytes(int64_t capacity)
+{
+    const int64_t C = capacity, S = 2 * capacity;
+    // per path: qo, qd x2 (64 B), qp x2 (8), hits 16, thr 16, rad 16, rng 8, pix 4, job 4,
+    // nee_val 64, pend 4; next-event queues: 2 x S x (so, sd, sv 48 B + sm 16 B);
+    // plus 256-B alignment of each of the 22 sub-arrays
+    return static_cast<size_t>(C) * (64 + 8 + 16 + 16 + 16 + 8 + 4 + 4 + 64 + 4) + static_cast<size_t>(S) * 2 * 64 +
+           256 * 24;
+}
+
+void carve_wave(WaveArgs& a, void* base, int64_t capacity)
+{
+    const int64_t C = capacity, S = 2 * capacity;
+    char*         p = static_cast<char*>(base);
+    auto          take = [&](size_t n) {
+        size_t off = (reinterpret_cast<uintptr_t>(p) + 255) & ~static_cast<uintptr_t>(255);
+        char*  r = reinterpret_cast<char*>(off);
+        p = r + n;
+        return static_cast<void*>(r);
+    };
+    for (int k = 0; k < 2; ++k)
+    {
+        a.qo[k] = static_cast<float4*>(take(16 * C));
+        a.qd[k] = static_cast<float4*>(take(16 * C));
+        a.qp[k] = static_cast<int*>(take(4 * C));
+    }
+    a.hits = static_cast<float4*>(take(16 * C));
+    a.thr = static_cast<float4*>(take(16 * C));
+    a.rad = static_cast<float4*>(take(16 * C));
+    a.rng = static_cast<uint64_t*>(take(8 * C));
+    a.pix = static_cast<int*>(take(4 * C));
+    a.job = static_cast<int*>(take(4 * C));
+    a.nee_val = static_cast<float4*>(take(64 * C));
+    a.pend = static_cast<int*>(take(4 * C));
+    for (int k = 0; k < 2; ++k)
+    {
+        a.so[k] = static_cast<float4*>(take(16 * S));
+        a.sd[k] = static_cast<float4*>(take(16 * S));
+        a.sv[k] = static_cast<float4*>(take(16 * S));
+        a.sm[k] = static_cast<int4*>(take(16 * S));
+    }
+    a.capacity = C;
+    a.shadow_cap = S;
+}
+
+LaunchShape launch_shape()
+{
+    LaunchShape ls;
+    int         sms = num_sms();
+    int         occ_t = 0, occ_s = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend<kStack, false>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 128, 0);
+    ls.grid_trace = sms * std::max(occ_t, 1);
+    ls.grid_shade = sms * std::max(occ_s, 1);
+    ls.grid_small = sms * 8;
+    ls.block = 128;
+    return ls;
+}
+
+void enqueue_wave_plain(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st)
+{
+    enqueue_wave<kStack, false>(a, max_depth, ls, st, nullptr);
+}
+
+CameraGPU make_camera(const mcrt_camera& c) { return make_camera_impl(c); }
+
+int validate_job(const mcrt_scene* s, const mcrt_camera* c, const mcrt_render_params* p)
+{
+    return validate_job_impl(s, c, p);
+}
+
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+
+const SceneView& scene_view(const mcrt_scene* s) { return s->view; }
+int              scene_device(const mcrt_scene* s) { return s->device; }
+int              scene_bvh_depth(const mcrt_scene* s) { return s->bvh_depth; }
+
+}  // namespace mcrt
 
 extern "C" {
 
@@ -1355,129 +1352,189 @@ int mcrt_render_batch(int32_t n, mcrt_scene* const* scenes, const mcrt_camera* c
     }
 }
 
+static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams,
+                        const mcrt_render_params* params, const float* const* dLs, float* d_albedo, int32_t n_albedo,
+                        float* d_emis, int32_t n_emis, mcrt_render_stats* stats, cudaStream_t st)
+{
+    if (num_jobs <= 0 || !scenes || !cams || !params || !dLs)
+        return fail(MCRT_ERR_INVALID_ARGUMENT, "empty adjoint batch");
+    const int ptr_mode = params[0].ptr_mode;
+    for (int j = 0; j < num_jobs; ++j)
+    {
+        int rc = validate_job_impl(scenes[j], &cams[j], &params[j]);
+        if (rc) return rc;
+        if (!dLs[j]) return fail(MCRT_ERR_INVALID_ARGUMENT, "null dL/dimage buffer");
+        if (params[j].ptr_mode != ptr_mode) return fail(MCRT_ERR_INVALID_ARGUMENT, "all jobs share ptr_mode");
+        if (scenes[j]->bvh_depth + 2 >= kStack) return fail(MCRT_ERR_STACK_OVERFLOW, "BVH deeper than the stack");
+    }
+    if ((n_albedo > 0 && !d_albedo) || (n_emis > 0 && !d_emis) || n_albedo < 0 || n_emis < 0)
+        return fail(MCRT_ERR_INVALID_ARGUMENT, "null gradient buffer");
+    mcrt_scene*                 owner = scenes[0];
+    std::lock_guard<std::mutex> lock(owner->mu);
+    CK(cudaSetDevice(owner->device));
+    std::vector<void*> temp;
+    auto               cleanup = [&]() {
+        for (void* t : temp) cudaFree(t);
+    };
+    auto dev_alloc = [&](size_t bytes) -> void* {
+        void* d = nullptr;
+        if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+        temp.push_back(d);
+        return d;
+    };
+    std::vector<JobGPU> jobs(num_jobs);
+    int64_t             total = 0;
+    int64_t             h2d = 0, d2h = 0;
+    for (int j = 0; j < num_jobs; ++j)
+    {
+        const mcrt_camera&        c = cams[j];
+        const mcrt_render_params& p = params[j];
+        JobGPU&                   J = jobs[j];
+        J.scene = scenes[j]->view;
+        J.cam = make_camera_impl(c);
+        J.width = c.width;
+        J.height = c.height;
+        J.spp = p.spp;
+        J.max_depth = p.max_depth;
+        J.rr_depth = p.rr_depth;
+        J.traverse = p.traverse;
+        J.seed = p.seed;
+        J.path_offset = total;
+        int64_t px = static_cast<int64_t>(c.width) * c.height;
+        total += px * p.spp;
+        if (ptr_mode == MCRT_PTR_DEVICE)
+        {
+            J.image = const_cast<float*>(dLs[j]);
+        }
+        else
+        {
+            void* d = dev_alloc(sizeof(float) * 3 * px);
+            if (!d)
+            {
+                cleanup();
+                return fail(MCRT_ERR_OUT_OF_MEMORY, "adjoint buffer allocation failed");
+            }
+            CK(cudaMemcpyAsync(d, dLs[j], sizeof(float) * 3 * px, cudaMemcpyHostToDevice, st));
+            h2d += static_cast<int64_t>(sizeof(float) * 3 * px);
+            J.image = static_cast<float*>(d);
+        }
+    }
+    float* dga = d_albedo;
+    float* dge = d_emis;
+    if (ptr_mode != MCRT_PTR_DEVICE)
+    {
+        void* a2 = dev_alloc(sizeof(float) * 3 * std::max(n_albedo, 1));
+        void* a3 = dev_alloc(sizeof(float) * 3 * std::max(n_emis, 1));
+        if (!a2 || !a3)
+        {
+            cleanup();
+            return fail(MCRT_ERR_OUT_OF_MEMORY, "adjoint buffer allocation failed");
+        }
+        if (n_albedo > 0) CK(cudaMemcpyAsync(a2, d_albedo, sizeof(float) * 3 * n_albedo, cudaMemcpyHostToDevice, st));
+        if (n_emis > 0) CK(cudaMemcpyAsync(a3, d_emis, sizeof(float) * 3 * n_emis, cudaMemcpyHostToDevice, st));
+        h2d += sizeof(float) * 3 * (n_albedo + n_emis);
+        dga = static_cast<float*>(a2);
+        dge = static_cast<float*>(a3);
+    }
+    Workspace& w = owner->ws;
+    int        rc = ensure_workspace(w, 64, num_jobs, 1);
+    if (rc)
+    {
+        cleanup();
+        return rc;
+    }
+    CK(cudaMemcpyAsync(w.jobs, jobs.data(), sizeof(JobGPU) * num_jobs, cudaMemcpyHostToDevice, st));
+    h2d += static_cast<int64_t>(sizeof(JobGPU)) * num_jobs;
+    CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
+    CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
+    AdjointArgs aa;
+    aa.jobs = w.jobs;
+    aa.num_jobs = num_jobs;
+    aa.g_albedo = dga;
+    aa.n_albedo = n_albedo;
+    aa.g_emis = dge;
+    aa.n_emis = n_emis;
+    aa.total_paths = total;
+    aa.stats = w.stats;
+    aa.err = w.err;
+    size_t gbytes = sizeof(float) * 3 * static_cast<size_t>(n_albedo + n_emis);
+    aa.shared_grads = gbytes <= 96 * 1024 ? 1 : 0;
+    size_t dyn = aa.shared_grads ? gbytes : 0;
+    if (dyn > 48 * 1024)
+        CK(cudaFuncSetAttribute(k_adjoint<kStack>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint<kStack>, kAdjBlock, dyn);
+    int64_t want = (total + kAdjBlock - 1) / kAdjBlock;
+    int     grid = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(num_sms()) * std::max(occ, 1)));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, st));
+    k_adjoint<kStack><<<grid, kAdjBlock, dyn, st>>>(aa);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(e1, st));
+    if (ptr_mode != MCRT_PTR_DEVICE)
+    {
+        if (n_albedo > 0) CK(cudaMemcpyAsync(d_albedo, dga, sizeof(float) * 3 * n_albedo, cudaMemcpyDeviceToHost, st));
+        if (n_emis > 0) CK(cudaMemcpyAsync(d_emis, dge, sizeof(float) * 3 * n_emis, cudaMemcpyDeviceToHost, st));
+        d2h += sizeof(float) * 3 * (n_albedo + n_emis);
+    }
+    unsigned long long hstats[8];
+    int                herr = 0;
+    CK(cudaMemcpyAsync(hstats, w.stats, sizeof(hstats), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&herr, w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    d2h += sizeof(hstats) + sizeof(herr);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cleanup();
+    if (stats)
+    {
+        *stats = mcrt_render_stats{};
+        stats->paths = total;
+        stats->extension_rays = static_cast<int64_t>(hstats[0]);
+        stats->waves = 1;
+        stats->kernel_launches = 1;
+        stats->device_ms = ms;
+        stats->h2d_bytes = h2d;
+        stats->d2h_bytes = d2h;
+    }
+    if (herr & kErrStack) return fail(MCRT_ERR_STACK_OVERFLOW, "traversal stack overflow");
+    return MCRT_OK;
+}
+
 int mcrt_render_adjoint(mcrt_scene* s, const mcrt_camera* c, const mcrt_render_params* p, const float* dL,
                         float* d_albedo, int32_t n_albedo, float* d_emis, int32_t n_emis, mcrt_render_stats* stats,
                         void* stream)
 {
     try
     {
-        int rc = validate_job(s, c, p);
-        if (rc) return rc;
-        if (!dL || (n_albedo > 0 && !d_albedo) || (n_emis > 0 && !d_emis) || n_albedo < 0 || n_emis < 0)
-            return fail(MCRT_ERR_INVALID_ARGUMENT, "null gradient or dL/dimage buffer");
-        if (s->bvh_depth + 2 >= kStack) return fail(MCRT_ERR_STACK_OVERFLOW, "BVH deeper than the traversal stack");
-        std::lock_guard<std::mutex> lock(s->mu);
-        CK(cudaSetDevice(s->device));
-        cudaStream_t st = static_cast<cudaStream_t>(stream);
-        int64_t      px = static_cast<int64_t>(c->width) * c->height;
-        const float* d_dl = dL;
-        float*       dga = d_albedo;
-        float*       dge = d_emis;
-        std::vector<void*> temp;
-        auto cleanup = [&]() {
-            for (void* t : temp) cudaFree(t);
-        };
-        auto dev_alloc = [&](size_t bytes) -> void* {
-            void* d = nullptr;
-            if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
-            temp.push_back(d);
-            return d;
-        };
-        if (p->ptr_mode != MCRT_PTR_DEVICE)
-        {
-            void* a1 = dev_alloc(sizeof(float) * 3 * px);
-            void* a2 = dev_alloc(sizeof(float) * 3 * std::max(n_albedo, 1));
-            void* a3 = dev_alloc(sizeof(float) * 3 * std::max(n_emis, 1));
-            if (!a1 || !a2 || !a3)
-            {
-                cleanup();
-                return fail(MCRT_ERR_OUT_OF_MEMORY, "adjoint buffer allocation failed");
-            }
-            CK(cudaMemcpyAsync(a1, dL, sizeof(float) * 3 * px, cudaMemcpyHostToDevice, st));
-            if (n_albedo > 0)
-                CK(cudaMemcpyAsync(a2, d_albedo, sizeof(float) * 3 * n_albedo, cudaMemcpyHostToDevice, st));
-            if (n_emis > 0) CK(cudaMemcpyAsync(a3, d_emis, sizeof(float) * 3 * n_emis, cudaMemcpyHostToDevice, st));
-            d_dl = static_cast<const float*>(a1);
-            dga = static_cast<float*>(a2);
-            dge = static_cast<float*>(a3);
-        }
-        Workspace& w = s->ws;
-        rc = ensure_workspace(w, 64, 1, 1);
-        if (rc)
-        {
-            cleanup();
-            return rc;
-        }
-        CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
-        CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
-        AdjointArgs aa;
-        aa.job.scene = s->view;
-        aa.job.cam = make_camera(*c);
-        aa.job.width = c->width;
-        aa.job.height = c->height;
-        aa.job.spp = p->spp;
-        aa.job.max_depth = p->max_depth;
-        aa.job.rr_depth = p->rr_depth;
-        aa.job.traverse = p->traverse;
-        aa.job.seed = p->seed;
-        aa.job.path_offset = 0;
-        aa.job.image = nullptr;
-        aa.dLdI = d_dl;
-        aa.g_albedo = dga;
-        aa.n_albedo = n_albedo;
-        aa.g_emis = dge;
-        aa.n_emis = n_emis;
-        aa.total_paths = px * p->spp;
-        aa.stats = w.stats;
-        aa.err = w.err;
-        size_t gbytes = sizeof(float) * 3 * static_cast<size_t>(n_albedo + n_emis);
-        aa.shared_grads = gbytes <= 96 * 1024 ? 1 : 0;
-        size_t dyn = aa.shared_grads ? gbytes : 0;
-        if (dyn > 48 * 1024)
-            CK(cudaFuncSetAttribute(k_adjoint<kStack>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(dyn)));
-        int occ = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint<kStack>, kAdjBlock, dyn);
-        int64_t want = (aa.total_paths + kAdjBlock - 1) / kAdjBlock;
-        int     grid = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(num_sms()) * std::max(occ, 1)));
-        cudaEvent_t e0, e1;
-        CK(cudaEventCreate(&e0));
-        CK(cudaEventCreate(&e1));
-        CK(cudaEventRecord(e0, st));
-        k_adjoint<kStack><<<grid, kAdjBlock, dyn, st>>>(aa);
-        CK(cudaGetLastError());
-        CK(cudaEventRecord(e1, st));
-        if (p->ptr_mode != MCRT_PTR_DEVICE)
-        {
-            if (n_albedo > 0)
-                CK(cudaMemcpyAsync(d_albedo, dga, sizeof(float) * 3 * n_albedo, cudaMemcpyDeviceToHost, st));
-            if (n_emis > 0) CK(cudaMemcpyAsync(d_emis, dge, sizeof(float) * 3 * n_emis, cudaMemcpyDeviceToHost, st));
-        }
-        unsigned long long hstats[4];
-        int                herr = 0;
-        CK(cudaMemcpyAsync(hstats, w.stats, sizeof(hstats), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&herr, w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        cleanup();
-        if (stats)
-        {
-            stats->paths = aa.total_paths;
-            stats->extension_rays = static_cast<int64_t>(hstats[0]);
-            stats->shadow_rays = 0;
-            stats->waves = 1;
-            stats->kernel_launches = 1;
-            stats->device_ms = ms;
-        }
-        if (herr & kErrStack) return fail(MCRT_ERR_STACK_OVERFLOW, "traversal stack overflow");
-        return MCRT_OK;
+        if (!s || !c || !p) return fail(MCRT_ERR_INVALID_ARGUMENT, "null scene, camera or params");
+        const float* dls[1] = {dL};
+        return adjoint_jobs(1, &s, c, p, dls, d_albedo, n_albedo, d_emis, n_emis, stats,
+                            static_cast<cudaStream_t>(stream));
     }
     catch (...)
     {
         return fail(MCRT_ERR_INTERNAL, "unexpected exception in mcrt_render_adjoint");
+    }
+}
+
+int mcrt_render_adjoint_batch(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cameras,
+                              const mcrt_render_params* params, const float* const* dL_dimages, float* d_albedo,
+                              int32_t num_albedo_params, float* d_emission, int32_t num_emission_params,
+                              mcrt_render_stats* stats, void* stream)
+{
+    try
+    {
+        return adjoint_jobs(num_jobs, scenes, cameras, params, dL_dimages, d_albedo, num_albedo_params, d_emission,
+                            num_emission_params, stats, static_cast<cudaStream_t>(stream));
+    }
+    catch (...)
+    {
+        return fail(MCRT_ERR_INTERNAL, "unexpected exception in mcrt_render_adjoint_batch");
     }
 }
 

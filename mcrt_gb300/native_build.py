@@ -22,7 +22,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["kernels.cu"]
 CPP_SOURCES = ["bvh_build.cpp", "flatten.cpp", "scene_prep.cpp"]
-HEADERS = ["layout.h", "host.h", "device.cuh", "estimator.cuh"]
+HEADERS = ["layout.h", "host.h", "device.cuh", "estimator.cuh", "wavefront.h"]
 
 
 def _cuda_home() -> str:

@@ -293,3 +293,36 @@ def render_batch(scenes: list, cameras: list, params: list, outs: list | None = 
     N.check(lib.mcrt_render_batch(n, hs, cs, ps, ptrs, ctypes.byref(st), _stream_ptr() if device else None),
             "mcrt_render_batch")
     return outs, stats_dict(st)
+
+
+def render_adjoint_batch(scenes: list, cameras: list, params: list, dL_dimages: list, n_albedo: int,
+                         n_emission: int):
+    """Adjoint of render_batch: all jobs' paths replayed in one launch, gradients summed.
+    dL_dimages: numpy arrays (host mode) or CUDA tensors (device mode).
+    Returns (d_albedo (n_albedo, 3), d_emission (n_emission, 3), stats)."""
+    lib = N.load()
+    n = len(scenes)
+    hs = (ctypes.c_void_p * n)(*[s.handle.value for s in scenes])
+    cs = (N.Camera * n)(*[c.to_c() for c in cameras])
+    ps = (N.RenderParams * n)(*[make_params(**p) for p in params])
+    device = _is_torch(dL_dimages[0])
+    for k in range(n):
+        ps[k].ptr_mode = N.PTR_DEVICE if device else N.PTR_HOST
+    if device:
+        import torch
+        dls = [d.contiguous() for d in dL_dimages]
+        ptrs = (ctypes.c_void_p * n)(*[d.data_ptr() for d in dls])
+        dev = dls[0].device
+        ga = torch.zeros((max(n_albedo, 1), 3), dtype=torch.float32, device=dev)
+        ge = torch.zeros((max(n_emission, 1), 3), dtype=torch.float32, device=dev)
+        gap, gep, stream = ga.data_ptr(), ge.data_ptr(), _stream_ptr()
+    else:
+        dls = [np.ascontiguousarray(d, np.float32) for d in dL_dimages]
+        ptrs = (ctypes.c_void_p * n)(*[d.ctypes.data for d in dls])
+        ga = np.zeros((max(n_albedo, 1), 3), np.float32)
+        ge = np.zeros((max(n_emission, 1), 3), np.float32)
+        gap, gep, stream = ga.ctypes.data, ge.ctypes.data, None
+    st = N.RenderStats()
+    N.check(lib.mcrt_render_adjoint_batch(n, hs, cs, ps, ptrs, gap, n_albedo, gep, n_emission, ctypes.byref(st),
+                                          stream), "mcrt_render_adjoint_batch")
+    return ga[:n_albedo], ge[:n_emission], stats_dict(st)

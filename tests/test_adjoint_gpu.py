@@ -93,3 +93,23 @@ def test_adjoint_forward_time_ratio(cuda_device):
     sc.render_adjoint(big, SPP, DEPTH, dl, albedo.shape[0], 1, seed=1)
     ta = time.perf_counter() - t0
     assert (tf + ta) / tf <= 3.0, f"forward {tf * 1e3:.1f} ms, adjoint {ta * 1e3:.1f} ms"
+
+
+def test_batched_adjoint_equals_sum_of_single_adjoints(cuda_device):
+    """Several views of one scene in one adjoint launch: the summed gradient."""
+    from mcrt_gb300 import CameraDesc, render_adjoint_batch
+    desc, cam, albedo, emission, sc = _setup()
+    cams = [cam, CameraDesc(origin=(0.4, 0.2, 3.3), target=(0.0, -0.3, 0.0), width=24, height=20, fov_y=45.0)]
+    rng = np.random.default_rng(4)
+    dls = [rng.normal(size=(c.height, c.width, 3)).astype(np.float32) for c in cams]
+    params = [dict(spp=8, max_depth=DEPTH, seed=21), dict(spp=4, max_depth=DEPTH, seed=22)]
+    gab, geb, st = render_adjoint_batch([sc, sc], cams, params, dls, albedo.shape[0], 1)
+    ga = np.zeros_like(gab)
+    ge = np.zeros_like(geb)
+    for c, p, d in zip(cams, params, dls):
+        a, e, _ = sc.render_adjoint(c, p["spp"], p["max_depth"], d, albedo.shape[0], 1, seed=p["seed"])
+        ga += a
+        ge += e
+    np.testing.assert_allclose(gab, ga, rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(geb, ge, rtol=1e-4, atol=1e-5)
+    assert st["paths"] == 32 * 32 * 8 + 24 * 20 * 4
