@@ -90,6 +90,8 @@ EXPORTS = {
                               ctypes.POINTER(RenderStats), c_void_p]),
     "mcrt_render_adjoint": (c_int32, [c_void_p, ctypes.POINTER(Camera), ctypes.POINTER(RenderParams), c_void_p,
                                       c_void_p, c_int32, c_void_p, c_int32, ctypes.POINTER(RenderStats), c_void_p]),
+    "mcrt_render_noalloc": (c_int32, [c_void_p, ctypes.POINTER(Camera), ctypes.POINTER(RenderParams), c_void_p,
+                                      ctypes.POINTER(RenderStats), c_void_p]),
     "mcrt_render_adjoint_batch": (c_int32, [c_int32, ctypes.POINTER(c_void_p), ctypes.POINTER(Camera),
                                             ctypes.POINTER(RenderParams), ctypes.POINTER(c_void_p), c_void_p, c_int32,
                                             c_void_p, c_int32, ctypes.POINTER(RenderStats), c_void_p]),
