@@ -152,13 +152,114 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _timed(fn, reps=1):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        r = fn()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / reps, r
+
+
+def bench_cfg2(args):
+    """64 procedural scenes of uneven size: one batched wavefront (CUDA graph per wave)
+    against the same renders issued scene by scene."""
+    import torch
+    from mcrt_gb300 import GpuScene, render_batch, scenes
+    jobs = scenes.cfg2_jobs(64)
+    t0 = time.time()
+    gs = [GpuScene(d) for d, _, _ in jobs]
+    setup_s = time.time() - t0
+    cams = [c for _, c, _ in jobs]
+    params = [dict(p, use_graph=True) for _, _, p in jobs]
+    outs = [torch.empty((c.height, c.width, 3), device="cuda") for c in cams]
+    render_batch(gs, cams, params, outs)  # warm-up
+    for s, c, p, o in zip(gs, cams, jobs, outs):
+        s.render(c, out=o, **p[2])
+    tb, (_, stb) = _timed(lambda: render_batch(gs, cams, params, outs), reps=args.steps)
+    def sequential():
+        tot = 0
+        for s, c, (_, _, p), o in zip(gs, cams, jobs, outs):
+            _, st = s.render(c, out=o, **p)
+            tot += st["rays"]
+        return tot
+    ts, seq_rays = _timed(sequential, reps=args.steps)
+    paths = stb["paths"]
+    line = {"workload": "cfg2: 64 scenes, displaced icospheres 1k-500k T in Cornell shells, res {128..1024}^2, "
+                        "spp 1..64, depth 4..16", "paths": paths, "rays": stb["rays"],
+            "batched_ms": round(tb * 1e3, 2), "sequential_ms": round(ts * 1e3, 2),
+            "batched_mrays_s": round(stb["rays"] / tb / 1e6, 1), "sequential_mrays_s": round(seq_rays / ts / 1e6, 1),
+            "batched_msamples_s": round(paths / tb / 1e6, 1), "speedup_batched_vs_sequential": round(ts / tb, 3),
+            "waves": stb["waves"], "scene_setup_s": round(setup_s, 1), "triangles": int(sum(d.num_triangles
+                                                                                               for d, _, _ in jobs))}
+    print(json.dumps(line), flush=True)
+
+
+def bench_cfg3(args):
+    """Differentiable Cornell box (256 albedo groups + emission), 512^2, 32 spp, depth 6:
+    forward time, forward+adjoint time."""
+    import torch
+    from mcrt_gb300 import GpuScene, scenes
+    desc, albedo, emission = scenes.cfg3_scene()
+    cam = scenes.cfg0_camera(512, 512)
+    sc = GpuScene(desc)
+    out = torch.empty((512, 512, 3), device="cuda")
+    kw = dict(spp=32, max_depth=6, seed=3)
+    dl = torch.randn((512, 512, 3), device="cuda")
+    sc.render(cam, out=out, **kw)
+    sc.render_adjoint(cam, 32, 6, dl, albedo.shape[0], 1, seed=3)
+    tf, (_, stf) = _timed(lambda: sc.render(cam, out=out, **kw), reps=args.steps)
+    ta, (_, _, sta) = _timed(lambda: sc.render_adjoint(cam, 32, 6, dl, albedo.shape[0], 1, seed=3), reps=args.steps)
+    line = {"workload": "cfg3: Cornell + 256 albedo groups + emission, 512x512, 32 spp, depth 6",
+            "forward_ms": round(tf * 1e3, 2), "adjoint_ms": round(ta * 1e3, 2),
+            "forward_plus_adjoint_over_forward": round((tf + ta) / tf, 3),
+            "forward_mrays_s": round(stf["rays"] / tf / 1e6, 1), "paths": stf["paths"]}
+    print(json.dumps(line), flush=True)
+
+
+def bench_cfg4(args):
+    """32 views of the 1.3 M-triangle scene, 256^2, 16 spp, depth 8, 4,096 albedo
+    parameters: batched forward + batched adjoint vs 32 sequential forward + adjoint."""
+    import torch
+    from mcrt_gb300 import GpuScene, render_adjoint_batch, render_batch, scenes
+    desc, albedo = scenes.cfg4_scene()
+    sc = GpuScene(desc)
+    cams = scenes.fibonacci_cameras(32)
+    p = dict(spp=16, max_depth=8, rr_depth=-1)
+    params = [dict(p, seed=100 + k, use_graph=True) for k in range(32)]
+    outs = [torch.empty((256, 256, 3), device="cuda") for _ in cams]
+    dls = [torch.randn((256, 256, 3), device="cuda") for _ in cams]
+    n = albedo.shape[0]
+
+    def batched():
+        render_batch([sc] * 32, cams, params, outs)
+        return render_adjoint_batch([sc] * 32, cams, [dict(p, seed=100 + k) for k in range(32)], dls, n, 0)
+
+    def sequential():
+        for k, c in enumerate(cams):
+            sc.render(c, out=outs[k], seed=100 + k, **p)
+            sc.render_adjoint(c, p["spp"], p["max_depth"], dls[k], n, 0, seed=100 + k)
+
+    batched()
+    sequential()
+    tb, _ = _timed(batched, reps=args.steps)
+    ts, _ = _timed(sequential, reps=args.steps)
+    tfb, _ = _timed(lambda: render_batch([sc] * 32, cams, params, outs), reps=args.steps)
+    line = {"workload": "cfg4: 32 Fibonacci views of the 1.3 M-T scene, 256x256, 16 spp, depth 8, 4096 albedos",
+            "batched_forward_adjoint_ms": round(tb * 1e3, 2), "sequential_forward_adjoint_ms": round(ts * 1e3, 2),
+            "speedup": round(ts / tb, 3), "batched_forward_ms": round(tfb * 1e3, 2),
+            "forward_plus_adjoint_over_forward": round(tb / tfb, 3)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg1", choices=["cfg1", "cfg0"])
+    ap.add_argument("--workload", default="cfg1", choices=["cfg1", "cfg0", "cfg2", "cfg3", "cfg4"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--traverse", default="fast", choices=["fast", "ref"])
     ap.add_argument("--res", type=int, default=0, help="override the resolution (profiling small cases)")
@@ -166,6 +267,9 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload in ("cfg2", "cfg3", "cfg4"):
+        {"cfg2": bench_cfg2, "cfg3": bench_cfg3, "cfg4": bench_cfg4}[args.workload](args)
         return
 
     import numpy as np

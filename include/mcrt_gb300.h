@@ -140,7 +140,14 @@ typedef struct mcrt_render_params {
     int32_t  block_size;  /* threads per block of the wavefront kernels, 0 -> default */
     int32_t  use_graph;   /* capture each wave's per-stage kernels in a CUDA graph */
     int32_t  profile;     /* MCRT_PROFILE_* bits (diagnostics; off for production renders) */
+    int32_t  variant;     /* traversal kernel variant, MCRT_VARIANT_* bits (0: default) */
 } mcrt_render_params;
+
+/* variant 0 = default policy (STACK32 when the BVH is shallow enough, REGCAP);
+ * MCRT_VARIANT_EXPLICIT | bits = exactly the given bits (for tuning) */
+#define MCRT_VARIANT_STACK32 1  /* 32-entry shared-memory stacks (16 KB/block) when the BVH is shallow enough */
+#define MCRT_VARIANT_REGCAP 2   /* cap registers at 64 so 8 blocks of 128 threads fit an SM */
+#define MCRT_VARIANT_EXPLICIT 4 /* use the bits as given instead of the default policy */
 
 #define MCRT_PROFILE_STAGES 1 /* CUDA events around every stage launch -> stats.stage_ms */
 #define MCRT_PROFILE_COUNT 2  /* count BVH nodes fetched / triangles tested per ray class */

@@ -29,6 +29,9 @@ PTR_HOST = 0
 PTR_DEVICE = 1
 PROFILE_STAGES = 1
 PROFILE_COUNT = 2
+VARIANT_STACK32 = 1
+VARIANT_REGCAP = 2
+VARIANT_EXPLICIT = 4
 BUILD_SAH = 0
 BUILD_EXTERNAL = 1
 
@@ -66,7 +69,7 @@ class Camera(ctypes.Structure):
 class RenderParams(ctypes.Structure):
     _fields_ = [("spp", c_int32), ("max_depth", c_int32), ("rr_depth", c_int32), ("seed", ctypes.c_uint64),
                 ("traverse", c_int32), ("ptr_mode", c_int32), ("path_chunk", c_int64), ("block_size", c_int32),
-                ("use_graph", c_int32), ("profile", c_int32)]
+                ("use_graph", c_int32), ("profile", c_int32), ("variant", c_int32)]
 
 
 class RenderStats(ctypes.Structure):

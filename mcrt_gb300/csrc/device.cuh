@@ -162,14 +162,16 @@ __device__ __forceinline__ bool watertight(const WatertightRay& r, float3 v0, fl
     return true;
 }
 
-// Two-child traversal over FastNode with a per-thread stack in shared memory
-// (`stack` points at this thread's column, entries `stride` ints apart).
 // Work counters of a traversal (MCRT_PROFILE_COUNT): nodes fetched, triangles tested.
 struct TraceCount
 {
     unsigned nodes, tris;
 };
 
+// Two-child traversal over FastNode with a per-thread stack in shared memory
+// (`stack` points at this thread's column, entries `stride` ints apart), nearer child
+// first.  (Postponing leaves until the whole warp holds one, Aila & Laine 2009, measured
+// slower on this GPU: 178 vs 132 ms of closest-hit traversal per cfg1 frame.)
 template <bool ANY, int STACK, bool COUNT = false>
 __device__ __forceinline__ bool trace_fast(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
                                            int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr)

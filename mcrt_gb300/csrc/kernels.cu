@@ -156,8 +156,8 @@ __device__ __forceinline__ float4 add_pending(const WaveArgs& a, int p, float4 r
     return r;
 }
 
-template <int STACK, bool COUNT>
-__global__ void __launch_bounds__(kTraceBlock) k_extend(WaveArgs a, int depth)
+template <int STACK, bool COUNT, int MINB>
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int depth)
 {
     __shared__ int stack[STACK * kTraceBlock];
     int*           st = stack + threadIdx.x;
@@ -319,8 +319,8 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
     }
 }
 
-template <int STACK, bool COUNT>
-__global__ void __launch_bounds__(kTraceBlock) k_connect(WaveArgs a, int depth)
+template <int STACK, bool COUNT, int MINB>
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, int depth)
 {
     __shared__ int stack[STACK * kTraceBlock];
     int*           st = stack + threadIdx.x;
@@ -771,7 +771,7 @@ struct StageTimer
     }
 };
 
-template <int STACK, bool COUNT>
+template <int STACK, bool COUNT, int MINB>
 void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st, StageTimer* tm)
 {
     auto beg = [&](int stg) {
@@ -787,13 +787,13 @@ void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaS
     for (int d = 0; d <= max_depth; ++d)
     {
         beg(1);
-        k_extend<STACK, COUNT><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
+        k_extend<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
         end();
         beg(2);
         k_shade<<<ls.grid_shade, 128, 0, st>>>(a, d);
         end();
         beg(3);
-        k_connect<STACK, COUNT><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
+        k_connect<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
         end();
     }
     beg(0);
@@ -929,8 +929,6 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
 
-    LaunchShape ls = launch_shape();
-
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -939,11 +937,31 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     const bool count = (p0.profile & MCRT_PROFILE_COUNT) != 0;
     const bool stages = (p0.profile & MCRT_PROFILE_STAGES) != 0;
     StageTimer timer;
-    auto       enqueue = [&](cudaStream_t s2, StageTimer* tm) {
-        if (count)
-            enqueue_wave<kStack, true>(w.args, max_depth, ls, s2, tm);
+    // variant 0: the default policy (32-entry stacks when the tree is shallow enough,
+    // registers capped for 8 blocks per SM); MCRT_VARIANT_EXPLICIT: the given bits
+    const int  vb = (p0.variant & MCRT_VARIANT_EXPLICIT) ? p0.variant : (MCRT_VARIANT_STACK32 | MCRT_VARIANT_REGCAP);
+    const bool stack32 = (vb & MCRT_VARIANT_STACK32) && bvh_depth + 2 < 32;
+    const bool regcap = (vb & MCRT_VARIANT_REGCAP) != 0;
+    LaunchShape lsv = launch_shape_variant(stack32, regcap);
+    auto        enqueue = [&](cudaStream_t s2, StageTimer* tm) {
+        if (stack32)
+        {
+            if (regcap)
+                count ? enqueue_wave<32, true, 8>(w.args, max_depth, lsv, s2, tm)
+                      : enqueue_wave<32, false, 8>(w.args, max_depth, lsv, s2, tm);
+            else
+                count ? enqueue_wave<32, true, 1>(w.args, max_depth, lsv, s2, tm)
+                      : enqueue_wave<32, false, 1>(w.args, max_depth, lsv, s2, tm);
+        }
         else
-            enqueue_wave<kStack, false>(w.args, max_depth, ls, s2, tm);
+        {
+            if (regcap)
+                count ? enqueue_wave<kStack, true, 8>(w.args, max_depth, lsv, s2, tm)
+                      : enqueue_wave<kStack, false, 8>(w.args, max_depth, lsv, s2, tm);
+            else
+                count ? enqueue_wave<kStack, true, 1>(w.args, max_depth, lsv, s2, tm)
+                      : enqueue_wave<kStack, false, 1>(w.args, max_depth, lsv, s2, tm);
+        }
     };
     if (p0.use_graph && !stages)
     {
@@ -1068,12 +1086,19 @@ void carve_wave(WaveArgs& a, void* base, int64_t capacity)
     a.shadow_cap = S;
 }
 
-LaunchShape launch_shape()
+LaunchShape launch_shape() { return launch_shape_variant(false, false); }
+
+LaunchShape launch_shape_variant(bool stack32, bool regcap)
 {
     LaunchShape ls;
     int         sms = num_sms();
     int         occ_t = 0, occ_s = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend<kStack, false>, kTraceBlock, 0);
+    if (stack32)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, regcap ? k_extend<32, false, 8> : k_extend<32, false, 1>,
+                                                      kTraceBlock, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ_t, regcap ? k_extend<kStack, false, 8> : k_extend<kStack, false, 1>, kTraceBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 128, 0);
     ls.grid_trace = sms * std::max(occ_t, 1);
     ls.grid_shade = sms * std::max(occ_s, 1);
@@ -1084,7 +1109,7 @@ LaunchShape launch_shape()
 
 void enqueue_wave_plain(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st)
 {
-    enqueue_wave<kStack, false>(a, max_depth, ls, st, nullptr);
+    enqueue_wave<kStack, false, 1>(a, max_depth, ls, st, nullptr);
 }
 
 CameraGPU make_camera(const mcrt_camera& c) { return make_camera_impl(c); }
@@ -1460,8 +1485,8 @@ static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_came
     size_t gbytes = sizeof(float) * 3 * static_cast<size_t>(n_albedo + n_emis);
     aa.shared_grads = gbytes <= 96 * 1024 ? 1 : 0;
     size_t dyn = aa.shared_grads ? gbytes : 0;
-    if (dyn > 48 * 1024)
-        CK(cudaFuncSetAttribute(k_adjoint<kStack>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
+    // the static traversal stack plus the gradient accumulators may exceed the 48 KB default
+    CK(cudaFuncSetAttribute(k_adjoint<kStack>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint<kStack>, kAdjBlock, dyn);
     int64_t want = (total + kAdjBlock - 1) / kAdjBlock;

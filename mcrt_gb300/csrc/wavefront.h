@@ -65,6 +65,7 @@ size_t wave_bytes(int64_t capacity);
 void carve_wave(WaveArgs& a, void* base, int64_t capacity);
 // persistent grid sizes from the SM count and occupancy (queries only, no allocation)
 LaunchShape launch_shape();
+LaunchShape launch_shape_variant(bool stack32, bool regcap);
 // one wave of stage launches on `st`: begin, raygen, (extend, shade, connect) x depth, resolve
 void enqueue_wave_plain(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st);
 // Camera::Camera in float with the reference's operation order
