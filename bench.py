@@ -172,16 +172,16 @@ def bench_cfg2(args):
     gs = [GpuScene(d) for d, _, _ in jobs]
     setup_s = time.time() - t0
     cams = [c for _, c, _ in jobs]
-    params = [dict(p, use_graph=True) for _, _, p in jobs]
+    params = [dict(p, use_graph=True, schedule=args.schedule_id) for _, _, p in jobs]
     outs = [torch.empty((c.height, c.width, 3), device="cuda") for c in cams]
     render_batch(gs, cams, params, outs)  # warm-up
     for s, c, p, o in zip(gs, cams, jobs, outs):
-        s.render(c, out=o, **p[2])
+        s.render(c, out=o, schedule=args.schedule_id, **p[2])
     tb, (_, stb) = _timed(lambda: render_batch(gs, cams, params, outs), reps=args.steps)
     def sequential():
         tot = 0
         for s, c, (_, _, p), o in zip(gs, cams, jobs, outs):
-            _, st = s.render(c, out=o, **p)
+            _, st = s.render(c, out=o, schedule=args.schedule_id, **p)
             tot += st["rays"]
         return tot
     ts, seq_rays = _timed(sequential, reps=args.steps)
@@ -191,7 +191,7 @@ def bench_cfg2(args):
             "batched_ms": round(tb * 1e3, 2), "sequential_ms": round(ts * 1e3, 2),
             "batched_mrays_s": round(stb["rays"] / tb / 1e6, 1), "sequential_mrays_s": round(seq_rays / ts / 1e6, 1),
             "batched_msamples_s": round(paths / tb / 1e6, 1), "speedup_batched_vs_sequential": round(ts / tb, 3),
-            "waves": stb["waves"], "scene_setup_s": round(setup_s, 1), "triangles": int(sum(d.num_triangles
+            "schedule": args.schedule, "waves": stb["waves"], "scene_setup_s": round(setup_s, 1), "triangles": int(sum(d.num_triangles
                                                                                                for d, _, _ in jobs))}
     print(json.dumps(line), flush=True)
 
@@ -205,7 +205,7 @@ def bench_cfg3(args):
     cam = scenes.cfg0_camera(512, 512)
     sc = GpuScene(desc)
     out = torch.empty((512, 512, 3), device="cuda")
-    kw = dict(spp=32, max_depth=6, seed=3)
+    kw = dict(spp=32, max_depth=6, seed=3, schedule=args.schedule_id)
     dl = torch.randn((512, 512, 3), device="cuda")
     sc.render(cam, out=out, **kw)
     sc.render_adjoint(cam, 32, 6, dl, albedo.shape[0], 1, seed=3)
@@ -214,7 +214,7 @@ def bench_cfg3(args):
     line = {"workload": "cfg3: Cornell + 256 albedo groups + emission, 512x512, 32 spp, depth 6",
             "forward_ms": round(tf * 1e3, 2), "adjoint_ms": round(ta * 1e3, 2),
             "forward_plus_adjoint_over_forward": round((tf + ta) / tf, 3),
-            "forward_mrays_s": round(stf["rays"] / tf / 1e6, 1), "paths": stf["paths"]}
+            "forward_mrays_s": round(stf["rays"] / tf / 1e6, 1), "paths": stf["paths"], "schedule": args.schedule}
     print(json.dumps(line), flush=True)
 
 
@@ -227,7 +227,7 @@ def bench_cfg4(args):
     sc = GpuScene(desc)
     cams = scenes.fibonacci_cameras(32)
     p = dict(spp=16, max_depth=8, rr_depth=-1)
-    params = [dict(p, seed=100 + k, use_graph=True) for k in range(32)]
+    params = [dict(p, seed=100 + k, use_graph=True, schedule=args.schedule_id) for k in range(32)]
     outs = [torch.empty((256, 256, 3), device="cuda") for _ in cams]
     dls = [torch.randn((256, 256, 3), device="cuda") for _ in cams]
     n = albedo.shape[0]
@@ -238,7 +238,7 @@ def bench_cfg4(args):
 
     def sequential():
         for k, c in enumerate(cams):
-            sc.render(c, out=outs[k], seed=100 + k, **p)
+            sc.render(c, out=outs[k], seed=100 + k, schedule=args.schedule_id, **p)
             sc.render_adjoint(c, p["spp"], p["max_depth"], dls[k], n, 0, seed=100 + k)
 
     batched()
@@ -249,7 +249,7 @@ def bench_cfg4(args):
     line = {"workload": "cfg4: 32 Fibonacci views of the 1.3 M-T scene, 256x256, 16 spp, depth 8, 4096 albedos",
             "batched_forward_adjoint_ms": round(tb * 1e3, 2), "sequential_forward_adjoint_ms": round(ts * 1e3, 2),
             "speedup": round(ts / tb, 3), "batched_forward_ms": round(tfb * 1e3, 2),
-            "forward_plus_adjoint_over_forward": round(tb / tfb, 3)}
+            "forward_plus_adjoint_over_forward": round(tb / tfb, 3), "schedule": args.schedule}
     print(json.dumps(line), flush=True)
 
 
@@ -264,7 +264,11 @@ def main():
     ap.add_argument("--traverse", default="fast", choices=["fast", "ref"])
     ap.add_argument("--res", type=int, default=0, help="override the resolution (profiling small cases)")
     ap.add_argument("--spp", type=int, default=0, help="override spp (profiling small cases)")
+    ap.add_argument("--schedule", default="stream", choices=["stream", "waves"],
+                    help="stream: slots refilled with new paths as paths end; waves: fixed waves")
+    ap.add_argument("--path-chunk", type=int, default=0, help="path slots in flight (0: library default)")
     args = ap.parse_args()
+    args.schedule_id = 0 if args.schedule == "stream" else 1
     if args.impl == "reference":
         run_reference(args)
         return
@@ -303,7 +307,8 @@ def main():
     traverse = TRAVERSE_FAST if args.traverse == "fast" else TRAVERSE_REF
     out = torch.empty((cam.height, cam.width, 3), dtype=torch.float32, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
-    kw = dict(spp=p["spp"], max_depth=p["max_depth"], rr_depth=p["rr_depth"], traverse=traverse)
+    kw = dict(spp=p["spp"], max_depth=p["max_depth"], rr_depth=p["rr_depth"], traverse=traverse,
+              schedule=args.schedule_id, path_chunk=args.path_chunk)
 
     def barrier():
         if dist:
@@ -347,7 +352,8 @@ def main():
     # algorithmic bytes of the two traversal kernels: a counting render of the same seeds.
     # k_extend per extension ray: 64 B per node, 48 B per triangle tested, 32 B ray + 16 B hit;
     # k_connect per next-event ray: nodes/triangles as above, 64 B ray + payload + meta in,
-    # 16 B result out.  Both kernels launch once per depth per wave.
+    # 16 B result out.  Both kernels launch once per depth per wave (waves) or once per
+    # iteration (streaming).
     _, sc_cnt = sc.render(cam, seed=0, out=out, profile=PROFILE_COUNT, **kw)
     ext_bytes = 64 * sc_cnt["ext_nodes"] + 48 * sc_cnt["ext_tris"] + (32 + 16) * sc_cnt["extension_rays"]
     nee_bytes = 64 * sc_cnt["nee_nodes"] + 48 * sc_cnt["nee_tris"] + (64 + 16) * sc_cnt["shadow_rays"]
@@ -398,7 +404,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scene, seeded)",
             "config": {"workload": text, "traversal": args.traverse, "l2": "flushed between steps (256 MB write)",
-                       "parallelism": f"replicas x{world}", "waves_per_step": st_last["waves"],
+                       "parallelism": f"replicas x{world}", "schedule": args.schedule,
+                       "path_slots": args.path_chunk or "default",
+                       "waves_or_iterations_per_step": st_last["waves"],
                        "scene_setup_s": round(setup_s, 2)},
             "msamples_per_s": round(msamples, 3),
             "rays_per_path": round(rays / max(paths, 1), 3),

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define MCRT_ABI_VERSION 1
+#define MCRT_ABI_VERSION 2
 
 /* status codes */
 #define MCRT_OK 0
@@ -136,12 +136,23 @@ typedef struct mcrt_render_params {
     uint64_t seed;
     int32_t  traverse;    /* MCRT_TRAVERSE_* for every ray of the render */
     int32_t  ptr_mode;    /* MCRT_PTR_* for image / gradient buffers */
-    int64_t  path_chunk;  /* paths in flight per wave, 0 -> library default */
+    int64_t  path_chunk;  /* path slots in flight (both schedules), 0 -> library default */
     int32_t  block_size;  /* threads per block of the wavefront kernels, 0 -> default */
     int32_t  use_graph;   /* capture each wave's per-stage kernels in a CUDA graph */
     int32_t  profile;     /* MCRT_PROFILE_* bits (diagnostics; off for production renders) */
     int32_t  variant;     /* traversal kernel variant, MCRT_VARIANT_* bits (0: default) */
+    int32_t  schedule;    /* MCRT_SCHEDULE_* (0: streaming) */
+    int32_t  reserved;    /* must be 0 */
 } mcrt_render_params;
+
+/* How paths are fed to the stage kernels.  Both give bit-identical images.
+ * STREAM: path_chunk slots; a slot whose path ended starts the next camera path in the
+ *   following iteration, so the queues stay full until the last paths; per-path results
+ *   go to a ring and each pixel is resolved (in sample order) when its last path ends.
+ * WAVES:  path_chunk paths per wave, every wave runs depth 0..max_depth to completion
+ *   before the next starts (the queues shrink with depth). */
+#define MCRT_SCHEDULE_STREAM 0
+#define MCRT_SCHEDULE_WAVES 1
 
 /* variant 0 = default policy (STACK32 when the BVH is shallow enough, REGCAP);
  * MCRT_VARIANT_EXPLICIT | bits = exactly the given bits (for tuning) */
@@ -156,7 +167,7 @@ typedef struct mcrt_render_stats {
     int64_t paths;
     int64_t extension_rays;
     int64_t shadow_rays;
-    int32_t waves;
+    int32_t waves;       /* WAVES: waves; STREAM: iterations (regen + extend + shade + connect) */
     int32_t kernel_launches;
     float   device_ms;   /* CUDA-event time of the kernels (excludes host copies) */
     float   stage_ms[4]; /* MCRT_PROFILE_STAGES: begin+raygen+resolve, extend, shade, connect */
@@ -222,7 +233,8 @@ int mcrt_render_batch(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_ca
  * allocation constraints).  For callers that cannot call cudaMalloc while rendering --
  * code recording a CUDA graph (allocation is not capturable), plug-ins confined to a host
  * application's own memory pool, callers under a fixed memory budget.  Same result as
- * mcrt_render with ptr_mode = MCRT_PTR_DEVICE; rgb_out must be device memory.
+ * mcrt_render with ptr_mode = MCRT_PTR_DEVICE; rgb_out must be device memory.  It always
+ * runs the WAVES schedule (params->schedule and params->path_chunk are not used).
  * Scratch: one fixed file-scope device array of about 31 MB, held by every GPU that loads
  * the library's module until the process exits; at most 65,536 path slots per wave
  * (spp <= 65,536) and 65,536 waves per call, larger requests fail with

@@ -32,6 +32,8 @@ PROFILE_COUNT = 2
 VARIANT_STACK32 = 1
 VARIANT_REGCAP = 2
 VARIANT_EXPLICIT = 4
+SCHEDULE_STREAM = 0
+SCHEDULE_WAVES = 1
 BUILD_SAH = 0
 BUILD_EXTERNAL = 1
 
@@ -69,7 +71,8 @@ class Camera(ctypes.Structure):
 class RenderParams(ctypes.Structure):
     _fields_ = [("spp", c_int32), ("max_depth", c_int32), ("rr_depth", c_int32), ("seed", ctypes.c_uint64),
                 ("traverse", c_int32), ("ptr_mode", c_int32), ("path_chunk", c_int64), ("block_size", c_int32),
-                ("use_graph", c_int32), ("profile", c_int32), ("variant", c_int32)]
+                ("use_graph", c_int32), ("profile", c_int32), ("variant", c_int32), ("schedule", c_int32),
+                ("reserved", c_int32)]
 
 
 class RenderStats(ctypes.Structure):

@@ -103,42 +103,46 @@ __global__ void k_begin_chunk(WaveArgs a)
     c->chunk = idx + 1;
 }
 
+// starts camera path g (sample s of pixel x, y of its job) in path slot `slot` and puts
+// its primary ray at position `pos` of ray queue `qsel` (demo_pt.cpp:689-700)
+__device__ __forceinline__ void start_camera_path(const WaveArgs& a, int64_t g, int slot, int qsel, int pos)
+{
+    int           j = find_job(a.jobs, a.num_jobs, g);
+    const JobGPU& J = a.jobs[j];
+    int64_t       local = g - J.path_offset;
+    int           pixel = static_cast<int>(local / J.spp);
+    int           s = static_cast<int>(local - static_cast<int64_t>(pixel) * J.spp);
+    int           x = pixel % J.width, y = pixel / J.width;
+    Pcg           rng;
+    rng.seed(J.seed, static_cast<uint32_t>(pixel), static_cast<uint32_t>(s));
+    float r1 = 2.f * rng.uniform();
+    float r2 = 2.f * rng.uniform();
+    float dx = 0.f, dy = 0.f;
+    if (J.spp > 1)
+    {
+        dx = tent(r1);
+        dy = tent(r2);
+    }
+    float3 o, d;
+    camera_ray(J.cam, (static_cast<float>(x) + 0.5f + dx) / static_cast<float>(J.width),
+               (static_cast<float>(y) + 0.5f + dy) / static_cast<float>(J.height), o, d);
+    a.qo[qsel][pos] = make_float4(o.x, o.y, o.z, kEpsRay);
+    a.qd[qsel][pos] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
+    a.qp[qsel][pos] = slot;
+    a.thr[slot] = make_float4(1.f, 1.f, 1.f, __int_as_float(0));  // flags 0, vertex 0
+    a.rad[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    a.rng[slot] = rng.state;
+    a.pix[slot] = pixel;
+    a.job[slot] = j;
+    a.pend[slot] = 0;
+}
+
 __global__ void k_raygen(WaveArgs a)
 {
     const int     count = a.ctrl->count;
     const int64_t base = a.ctrl->base;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x)
-    {
-        int64_t       g = base + p;
-        int           j = find_job(a.jobs, a.num_jobs, g);
-        const JobGPU& J = a.jobs[j];
-        int64_t       local = g - J.path_offset;
-        int           pixel = static_cast<int>(local / J.spp);
-        int           s = static_cast<int>(local - static_cast<int64_t>(pixel) * J.spp);
-        int           x = pixel % J.width, y = pixel / J.width;
-        Pcg           rng;
-        rng.seed(J.seed, static_cast<uint32_t>(pixel), static_cast<uint32_t>(s));
-        float r1 = 2.f * rng.uniform();
-        float r2 = 2.f * rng.uniform();
-        float dx = 0.f, dy = 0.f;
-        if (J.spp > 1)
-        {
-            dx = tent(r1);
-            dy = tent(r2);
-        }
-        float3 o, d;
-        camera_ray(J.cam, (static_cast<float>(x) + 0.5f + dx) / static_cast<float>(J.width),
-                   (static_cast<float>(y) + 0.5f + dy) / static_cast<float>(J.height), o, d);
-        a.qo[0][p] = make_float4(o.x, o.y, o.z, kEpsRay);
-        a.qd[0][p] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
-        a.qp[0][p] = p;
-        a.thr[p] = make_float4(1.f, 1.f, 1.f, __int_as_float(0));
-        a.rad[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-        a.rng[p] = rng.state;
-        a.pix[p] = pixel;
-        a.job[p] = j;
-        a.pend[p] = 0;
-    }
+        start_camera_path(a, base + p, p, 0, p);
 }
 
 // adds a path's pending next-event results in slot order (deterministic sum)
@@ -157,12 +161,11 @@ __device__ __forceinline__ float4 add_pending(const WaveArgs& a, int p, float4 r
 }
 
 template <int STACK, bool COUNT, int MINB>
-__global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int depth)
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, const int* count, int qs)
 {
     __shared__ int stack[STACK * kTraceBlock];
     int*           st = stack + threadIdx.x;
-    const int      n = a.ctrl->qcount[depth];
-    const int      qs = depth & 1;
+    const int      n = min(*count, static_cast<int>(a.capacity));
     TraceCount     cnt = {0u, 0u};
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[0], static_cast<unsigned long long>(n));
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -204,10 +207,10 @@ __device__ __forceinline__ int warp_append(int* counter, int k)
     return base + incl - k;
 }
 
-__global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
+__global__ void __launch_bounds__(128) k_shade(WaveArgs a, QueueSel q)
 {
-    const int n = a.ctrl->qcount[depth];
-    const int qs = depth & 1;
+    const int n = min(*q.count, static_cast<int>(a.capacity));
+    const int qs = q.qs;
     const int lane = threadIdx.x & 31;
     const int warps_total = (gridDim.x * blockDim.x) >> 5;
     for (int wbase = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < n; wbase += warps_total * 32)
@@ -216,7 +219,7 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
         bool valid = i < n;
         bool     cont = false;
         float3   phit = mk(0.f, 0.f, 0.f), cdir = mk(0.f, 0.f, 1.f), T2 = mk(0.f, 0.f, 0.f);
-        int      flags2 = 0, n_nee = 0, p = 0;
+        int      flags2 = 0, n_nee = 0, p = 0, depth = 0;
         uint64_t rstate = 0;
         NeeRay   nee[4];
         if (valid)
@@ -229,6 +232,7 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
             const SceneView& S = J.scene;
             float4           t4 = a.thr[p];
             float3           T = xyz(t4);
+            depth = q.depth >= 0 ? q.depth : (__float_as_int(t4.w) >> 8);
             bool             no_direct = depth == 0 || !(__float_as_int(t4.w) & 1);
             int              prim = __float_as_int(hh.w);
             float3           Ladd = mk(0.f, 0.f, 0.f);
@@ -261,7 +265,7 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
                     bool   nee_here = does_nee(m.type);
                     if (nee_here) n_nee = make_nee(S, m, wi, ns, phit, T, u, nee);
                     cont = continue_path(m, wi, ns, T, u, depth, J.max_depth, J.rr_depth, T2, cdir);
-                    flags2 = nee_here ? 1 : 0;
+                    flags2 = (nee_here ? 1 : 0) | ((depth + 1) << 8);
                 }
             }
             a.rad[p] = make_float4(rp.x + Ladd.x, rp.y + Ladd.y, rp.z + Ladd.z, rp.w);
@@ -272,7 +276,7 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
         if (live)
         {
             int base = 0;
-            if (lane == 0) base = atomicAdd(&a.ctrl->qcount[depth + 1], __popc(live));
+            if (lane == 0) base = atomicAdd(q.next_count, __popc(live));
             base = __shfl_sync(0xffffffffu, base, 0);
             if (cont)
             {
@@ -292,6 +296,25 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
                 }
             }
         }
+        // streaming: slots whose path ended are listed for the next iteration's k_regen
+        if (q.dead)
+        {
+            unsigned fin = __ballot_sync(0xffffffffu, valid && !cont);
+            if (fin)
+            {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(q.dead_count, __popc(fin));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (valid && !cont)
+                {
+                    int k = base + __popc(fin & lanemask_lt());
+                    if (k < a.capacity)
+                        q.dead[k] = p;
+                    else
+                        atomicOr(a.err, kErrQueue);
+                }
+            }
+        }
         // next-event rays: any-hit queue [0], closest-hit queue [1] (warp prefix sums)
         int n_any = 0;
         for (int r = 0; r < n_nee; ++r) n_any += nee[r].type == NEE_ENV ? 1 : 0;
@@ -299,7 +322,7 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
         for (int qsel = 0; qsel < 2; ++qsel)
         {
             int k = qsel == 0 ? n_any : n_cl;
-            int b = warp_append(&a.ctrl->scount[depth][qsel], k);
+            int b = warp_append(&q.scount[qsel], k);
             int w = 0;
             for (int r = 0; r < n_nee; ++r)
             {
@@ -320,13 +343,13 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int depth)
 }
 
 template <int STACK, bool COUNT, int MINB>
-__global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, int depth)
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, const int* counts)
 {
     __shared__ int stack[STACK * kTraceBlock];
     int*           st = stack + threadIdx.x;
     TraceCount     cnt = {0u, 0u};
-    const int      n0 = a.ctrl->scount[depth][0];
-    const int      n1 = a.ctrl->scount[depth][1];
+    const int      n0 = min(counts[0], static_cast<int>(a.shadow_cap));
+    const int      n1 = min(counts[1], static_cast<int>(a.shadow_cap));
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[1], static_cast<unsigned long long>(n0 + n1));
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0 + n1; i += gridDim.x * blockDim.x)
     {
@@ -557,6 +580,114 @@ __global__ void k_resolve(WaveArgs a)
     }
 }
 
+// ---------------------------------------------------------------------------
+// streaming schedule (path regeneration).  Per iteration, with parity par:
+//   k_stream_begin  zero the counters the iteration appends to
+//   k_regen         slots listed dead[par] (their path ended in the previous iteration's
+//                   k_shade, its next-event results are in): store the path's radiance
+//                   in the ring, resolve its pixel if that was the pixel's last path, and
+//                   start the next camera path in the slot (ray queue par)
+//   k_extend, k_shade, k_connect on ray queue par; k_shade appends continuing rays to
+//                   queue par ^ 1 and the slots of ended paths to dead[par ^ 1]
+// A slot starts at most one path per iteration and a path needs at most max_depth + 2
+// iterations from start to ring, so with C slots the paths whose ring entries are live
+// span fewer than (max_depth + 2) * C + spp indices: a ring of that size never
+// overwrites an entry before its pixel is resolved.
+// ---------------------------------------------------------------------------
+__global__ void k_stream_init(WaveArgs a, StreamArgs s)
+{
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < a.capacity;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        s.dead[0][i] = static_cast<int>(i);
+        s.gid[i] = -1;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.ctrl->dcount[0] = static_cast<int>(a.capacity);
+}
+
+__global__ void k_stream_begin(StreamArgs s, int par)
+{
+    s.ctrl->qcount[par ^ 1] = 0;
+    s.ctrl->dcount[par ^ 1] = 0;
+    s.ctrl->scount[0] = 0;
+    s.ctrl->scount[1] = 0;
+}
+
+// stores the radiance of path g (held by `slot`) in the ring; the call that stores the
+// last path of a pixel resolves the pixel from the ring in sample order, with the
+// arithmetic of k_resolve
+__device__ __forceinline__ void finish_path(const WaveArgs& a, const StreamArgs& s, int slot, int64_t g)
+{
+    float4        r = add_pending(a, slot, a.rad[slot]);
+    const JobGPU& J = a.jobs[a.job[slot]];
+    const int64_t R = s.ring_size;
+    const int     pixel = a.pix[slot];
+    const int64_t first = J.path_offset + static_cast<int64_t>(pixel) * J.spp;
+    s.ring[g % R] = r;
+    __threadfence();  // the entry is visible before the count that announces it
+    const int64_t c = first % R;
+    if (atomicAdd(&s.ring_cnt[c], 1) != J.spp - 1) return;
+    __threadfence();
+    s.ring_cnt[c] = 0;
+    float   acc[3] = {0.f, 0.f, 0.f};
+    int64_t idx = c;
+    for (int k = 0; k < J.spp; ++k)
+    {
+        float4 v = __ldcg(&s.ring[idx]);  // L2: written by other blocks of this launch
+        if (isnan3(xyz(v))) v = make_float4(0.f, 0.f, 0.f, 0.f);  // demo_pt.cpp:653
+        acc[0] += fmax_ref(0.f, v.x);                               // demo_pt.cpp:703
+        acc[1] += fmax_ref(0.f, v.y);
+        acc[2] += fmax_ref(0.f, v.z);
+        if (++idx == R) idx = 0;
+    }
+    float  scale = static_cast<float>(1.0 / J.spp);  // FrameBuffer::scale(1.0 / spp)
+    float* px = J.image + 3 * static_cast<int64_t>(pixel);
+    px[0] = acc[0] * scale;
+    px[1] = acc[1] * scale;
+    px[2] = acc[2] * scale;
+}
+
+__global__ void __launch_bounds__(128) k_regen(WaveArgs a, StreamArgs s, int par)
+{
+    const int          nd = min(s.ctrl->dcount[par], static_cast<int>(a.capacity));
+    const int          lane = threadIdx.x & 31;
+    const int          warps_total = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long fin = 0;
+    for (int wbase = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < nd; wbase += warps_total * 32)
+    {
+        const int  i = wbase + lane;
+        const bool valid = i < nd;
+        const int  slot = valid ? s.dead[par][i] : 0;
+        if (valid)
+        {
+            const int64_t g = s.gid[slot];
+            if (g >= 0)
+            {
+                finish_path(a, s, slot, g);
+                ++fin;
+            }
+        }
+        // the warp's slots take consecutive path indices (neighbouring samples)
+        const unsigned     want = __ballot_sync(0xffffffffu, valid);
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&s.ctrl->next, static_cast<unsigned long long>(__popc(want)));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const int64_t g = static_cast<int64_t>(base) + __popc(want & lanemask_lt());
+        const bool    start = valid && g < s.total;
+        const int     pos = warp_append(&s.ctrl->qcount[par], start ? 1 : 0);
+        if (valid) s.gid[slot] = start ? g : -1;
+        if (start)
+        {
+            if (pos < a.capacity)
+                start_camera_path(a, g, slot, par, pos);
+            else
+                atomicOr(a.err, kErrQueue);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) fin += __shfl_down_sync(0xffffffffu, fin, off);
+    if (lane == 0 && fin) atomicAdd(&s.ctrl->finished, fin);
+}
+
 }  // namespace mcrt
 
 // ===========================================================================
@@ -595,8 +726,26 @@ struct Workspace
     Ctrl*    ctrl = nullptr;
     unsigned long long* stats = nullptr;
     int*     err = nullptr;
+    // streaming schedule
+    int64_t             s_capacity = 0;  // slots of s_block (dead lists, gid)
+    int64_t             s_ring = 0;      // entries of s_ring_block (ring, ring_cnt)
+    void*               s_block = nullptr;
+    void*               s_ring_block = nullptr;
+    StreamCtrl*         s_ctrl = nullptr;
+    unsigned long long* h_poll = nullptr;  // pinned: completion polls
+    StreamArgs          sargs{};
     void release()
     {
+        cudaFree(s_block);
+        cudaFree(s_ring_block);
+        cudaFree(s_ctrl);
+        cudaFreeHost(h_poll);
+        s_block = nullptr;
+        s_ring_block = nullptr;
+        s_ctrl = nullptr;
+        h_poll = nullptr;
+        s_capacity = 0;
+        s_ring = 0;
         cudaFree(block);
         cudaFree(jobs);
         cudaFree(chunk_table);
@@ -787,17 +936,46 @@ void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaS
     for (int d = 0; d <= max_depth; ++d)
     {
         beg(1);
-        k_extend<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
+        k_extend<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, &a.ctrl->qcount[d], d & 1);
         end();
         beg(2);
-        k_shade<<<ls.grid_shade, 128, 0, st>>>(a, d);
+        QueueSel q{&a.ctrl->qcount[d], d & 1, &a.ctrl->qcount[d + 1], a.ctrl->scount[d], nullptr, nullptr, d};
+        k_shade<<<ls.grid_shade, 128, 0, st>>>(a, q);
         end();
         beg(3);
-        k_connect<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, d);
+        k_connect<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, a.ctrl->scount[d]);
         end();
     }
     beg(0);
     k_resolve<<<ls.grid_small, 256, 0, st>>>(a);
+    end();
+}
+
+// one streaming iteration of parity `par` (five launches)
+template <int STACK, bool COUNT, int MINB>
+void enqueue_stream_iter(const WaveArgs& a, const StreamArgs& x, int par, const LaunchShape& ls, cudaStream_t st,
+                         StageTimer* tm)
+{
+    auto beg = [&](int stg) {
+        if (tm) tm->record(st, stg, true);
+    };
+    auto end = [&]() {
+        if (tm) tm->record(st, 0, false);
+    };
+    beg(0);
+    k_stream_begin<<<1, 1, 0, st>>>(x, par);
+    k_regen<<<ls.grid_shade, 128, 0, st>>>(a, x, par);
+    end();
+    beg(1);
+    k_extend<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, &x.ctrl->qcount[par], par);
+    end();
+    beg(2);
+    QueueSel q{&x.ctrl->qcount[par], par, &x.ctrl->qcount[par ^ 1], x.ctrl->scount, &x.ctrl->dcount[par ^ 1],
+               x.dead[par ^ 1], -1};
+    k_shade<<<ls.grid_shade, 128, 0, st>>>(a, q);
+    end();
+    beg(3);
+    k_connect<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, x.ctrl->scount);
     end();
 }
 
@@ -812,6 +990,309 @@ int validate_job_impl(const mcrt_scene* s, const mcrt_camera* c, const mcrt_rend
         return fail(MCRT_ERR_INVALID_ARGUMENT, "unknown traversal mode");
     if (static_cast<int64_t>(c->width) * c->height > (int64_t(1) << 31) / 2)
         return fail(MCRT_ERR_INVALID_ARGUMENT, "image too large");
+    if (p->schedule != MCRT_SCHEDULE_STREAM && p->schedule != MCRT_SCHEDULE_WAVES)
+        return fail(MCRT_ERR_INVALID_ARGUMENT, "unknown schedule");
+    if (p->reserved != 0) return fail(MCRT_ERR_INVALID_ARGUMENT, "reserved field must be 0");
+    return MCRT_OK;
+}
+
+struct RunResult
+{
+    cudaEvent_t e0 = nullptr, e1 = nullptr;  // around the kernels
+    int64_t     waves = 0;                   // waves, or streaming iterations
+    int64_t     launches = 0;
+    int64_t     extend_launches = 0;
+    int64_t     table_bytes = 0;  // host -> device besides the job table
+    int64_t     poll_bytes = 0;   // device -> host completion polls
+};
+
+struct WaveEnqueue
+{
+    const WaveArgs*    a;
+    int                max_depth;
+    const LaunchShape* ls;
+    cudaStream_t       st;
+    StageTimer*        tm;
+    template <int S, bool C, int M>
+    void run() const
+    {
+        enqueue_wave<S, C, M>(*a, max_depth, *ls, st, tm);
+    }
+};
+
+struct StreamEnqueue
+{
+    const WaveArgs*    a;
+    const StreamArgs*  x;
+    int                par;
+    const LaunchShape* ls;
+    cudaStream_t       st;
+    StageTimer*        tm;
+    template <int S, bool C, int M>
+    void run() const
+    {
+        enqueue_stream_iter<S, C, M>(*a, *x, par, *ls, st, tm);
+    }
+};
+
+// dispatch of the traversal-kernel template variants
+template <class F>
+void with_variant(bool stack32, bool regcap, bool count, const F& f)
+{
+    if (stack32)
+    {
+        if (regcap)
+            count ? f.template run<32, true, 8>() : f.template run<32, false, 8>();
+        else
+            count ? f.template run<32, true, 1>() : f.template run<32, false, 1>();
+    }
+    else
+    {
+        if (regcap)
+            count ? f.template run<kStack, true, 8>() : f.template run<kStack, false, 8>();
+        else
+            count ? f.template run<kStack, true, 1>() : f.template run<kStack, false, 1>();
+    }
+}
+
+int begin_run(Workspace& w, const std::vector<JobGPU>& jobs, cudaStream_t st, RunResult& run)
+{
+    w.args.num_jobs = static_cast<int>(jobs.size());
+    CK(cudaMemcpyAsync(w.jobs, jobs.data(), sizeof(JobGPU) * jobs.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
+    CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
+    CK(cudaEventCreate(&run.e0));
+    CK(cudaEventCreate(&run.e1));
+    return MCRT_OK;
+}
+
+// WAVES: path_chunk paths per wave (wave boundaries on pixel boundaries so a pixel's
+// samples resolve together), each wave runs to completion
+int run_waves(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<int64_t>& pix_spp, int64_t total,
+              int max_depth, int64_t path_chunk, bool stack32, bool regcap, bool count, bool stages, bool graph,
+              const LaunchShape& lsv, cudaStream_t st, StageTimer& timer, RunResult& run)
+{
+    const int num_jobs = static_cast<int>(jobs.size());
+    int64_t   capacity = path_chunk > 0 ? path_chunk : (int64_t(1) << 22);
+    capacity = std::max<int64_t>(capacity, 64);
+    std::vector<int64_t> table;
+    table.push_back(0);
+    {
+        int64_t pos = 0;
+        int     j = 0;
+        while (pos < total)
+        {
+            int64_t end = std::min(total, pos + capacity);
+            while (j + 1 < num_jobs && jobs[j + 1].path_offset <= end - 1) ++j;
+            // job containing `end` (exclusive bound): round down to its pixel boundary
+            int jj = j;
+            while (jj + 1 < num_jobs && jobs[jj + 1].path_offset <= end) ++jj;
+            if (end < total)
+            {
+                int64_t local = end - jobs[jj].path_offset;
+                int64_t rounded = jobs[jj].path_offset + (local / pix_spp[jj]) * pix_spp[jj];
+                if (rounded <= pos)
+                {
+                    // one pixel larger than the capacity: extend to its end
+                    rounded = jobs[jj].path_offset + ((local + pix_spp[jj] - 1) / pix_spp[jj]) * pix_spp[jj];
+                }
+                end = rounded;
+            }
+            table.push_back(end);
+            pos = end;
+        }
+    }
+    const int64_t num_chunks = static_cast<int64_t>(table.size()) - 1;
+    int64_t       max_chunk = 0;
+    for (int64_t k = 0; k < num_chunks; ++k) max_chunk = std::max(max_chunk, table[k + 1] - table[k]);
+    int rc = ensure_workspace(w, max_chunk, num_jobs, num_chunks);
+    if (rc) return rc;
+    rc = begin_run(w, jobs, st, run);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(w.chunk_table, table.data(), sizeof(int64_t) * table.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(w.ctrl, 0, sizeof(Ctrl), st));
+    run.table_bytes = 8 * static_cast<int64_t>(table.size());
+    run.waves = num_chunks;
+    run.launches = num_chunks * (3 + 3 * (max_depth + 1));
+    run.extend_launches = num_chunks * (max_depth + 1);
+    const WaveArgs a = w.args;
+    auto enqueue = [&](cudaStream_t s2, StageTimer* tm) {
+        with_variant(stack32, regcap, count, WaveEnqueue{&a, max_depth, &lsv, s2, tm});
+    };
+    CK(cudaEventRecord(run.e0, st));
+    if (graph)
+    {
+        cudaGraph_t     g;
+        cudaGraphExec_t exec;
+        cudaStream_t    cap;
+        CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        enqueue(cap, nullptr);
+        CK(cudaStreamEndCapture(cap, &g));
+        CK(cudaGraphInstantiate(&exec, g, 0));
+        for (int64_t k = 0; k < num_chunks; ++k) CK(cudaGraphLaunch(exec, st));
+        CK(cudaEventRecord(run.e1, st));
+        CK(cudaStreamSynchronize(st));
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(g);
+        cudaStreamDestroy(cap);
+    }
+    else
+    {
+        for (int64_t k = 0; k < num_chunks; ++k) enqueue(st, stages ? &timer : nullptr);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(run.e1, st));
+    }
+    return MCRT_OK;
+}
+
+size_t align256(size_t n) { return (n + 255) & ~static_cast<size_t>(255); }
+
+int ensure_stream(Workspace& w, int64_t slots, int64_t ring)
+{
+    if (w.s_capacity < slots)
+    {
+        cudaFree(w.s_block);
+        w.s_block = nullptr;
+        w.s_capacity = 0;
+        CK(cudaMalloc(&w.s_block, 2 * align256(4 * slots) + align256(8 * slots)));
+        w.s_capacity = slots;
+    }
+    if (w.s_ring < ring)
+    {
+        cudaFree(w.s_ring_block);
+        w.s_ring_block = nullptr;
+        w.s_ring = 0;
+        CK(cudaMalloc(&w.s_ring_block, align256(16 * ring) + align256(4 * ring)));
+        w.s_ring = ring;
+    }
+    if (!w.s_ctrl)
+    {
+        CK(cudaMalloc(&w.s_ctrl, sizeof(StreamCtrl)));
+        CK(cudaMallocHost(&w.h_poll, 2 * sizeof(unsigned long long)));
+    }
+    char* b = static_cast<char*>(w.s_block);
+    w.sargs.ctrl = w.s_ctrl;
+    w.sargs.dead[0] = reinterpret_cast<int*>(b);
+    w.sargs.dead[1] = reinterpret_cast<int*>(b + align256(4 * w.s_capacity));
+    w.sargs.gid = reinterpret_cast<int64_t*>(b + 2 * align256(4 * w.s_capacity));
+    char* r = static_cast<char*>(w.s_ring_block);
+    w.sargs.ring = reinterpret_cast<float4*>(r);
+    w.sargs.ring_cnt = reinterpret_cast<int*>(r + align256(16 * w.s_ring));
+    return MCRT_OK;
+}
+
+// STREAM: path_chunk slots refilled with new camera paths as paths end (see k_regen);
+// iterations run in graph-launched pairs (parity 0, 1) until every path is in the ring,
+// which the host learns from a device counter polled one batch behind the launches
+int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<int64_t>& pix_spp, int64_t total,
+               int max_depth, int64_t path_chunk, bool stack32, bool regcap, bool count, bool stages, bool graph,
+               const LaunchShape& lsv, cudaStream_t st, StageTimer& timer, RunResult& run)
+{
+    const int num_jobs = static_cast<int>(jobs.size());
+    int64_t   slots = path_chunk > 0 ? path_chunk : (int64_t(1) << 21);
+    slots = std::min(slots, (total + 31) / 32 * 32);
+    slots = std::max<int64_t>(slots, 64);
+    if (slots > (int64_t(1) << 30)) return fail(MCRT_ERR_INVALID_ARGUMENT, "path_chunk too large");
+    int64_t max_spp = 1;
+    for (int64_t v : pix_spp) max_spp = std::max(max_spp, v);
+    const int64_t ring = std::min(total, (max_depth + 2) * slots + max_spp);
+    int           rc = ensure_workspace(w, slots, num_jobs, 0);
+    if (rc) return rc;
+    rc = ensure_stream(w, slots, ring);
+    if (rc) return rc;
+    rc = begin_run(w, jobs, st, run);
+    if (rc) return rc;
+    WaveArgs a = w.args;  // sub-arrays sized for >= slots; use exactly `slots`
+    a.capacity = slots;
+    a.shadow_cap = 2 * slots;
+    StreamArgs x = w.sargs;
+    x.ring_size = ring;
+    x.total = total;
+    CK(cudaMemsetAsync(x.ctrl, 0, sizeof(StreamCtrl), st));
+    CK(cudaMemsetAsync(x.ring_cnt, 0, sizeof(int) * ring, st));
+    auto iter = [&](cudaStream_t s2, int par, StageTimer* tm) {
+        with_variant(stack32, regcap, count, StreamEnqueue{&a, &x, par, &lsv, s2, tm});
+    };
+    // a slot holds one path for at most max_depth + 1 iterations and starts the next in
+    // the iteration that ends it: every path is in the ring after this many iterations
+    const int64_t bound = ((total + slots - 1) / slots + 1) * (max_depth + 1) + 2;
+    constexpr int kPairsPerPoll = 4;
+    CK(cudaEventRecord(run.e0, st));
+    k_stream_init<<<lsv.grid_small, 256, 0, st>>>(a, x);
+    run.launches = 1;
+    cudaGraph_t     g = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t    cap = nullptr;
+    auto            release_graph = [&]() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (g) cudaGraphDestroy(g);
+        if (cap) cudaStreamDestroy(cap);
+    };
+    if (graph)
+    {
+        CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        iter(cap, 0, nullptr);
+        iter(cap, 1, nullptr);
+        cudaError_t e = cudaStreamEndCapture(cap, &g);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+        if (e != cudaSuccess)
+        {
+            release_graph();
+            return fail(MCRT_ERR_CUDA, std::string("stream graph: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaEvent_t poll_ev[2];
+    CK(cudaEventCreateWithFlags(&poll_ev[0], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&poll_ev[1], cudaEventDisableTiming));
+    int64_t     iters = 0;
+    cudaError_t e = cudaSuccess;
+    bool        done = false;
+    for (int b = 0; !done && e == cudaSuccess; ++b)
+    {
+        for (int k = 0; k < kPairsPerPoll && e == cudaSuccess; ++k)
+        {
+            if (graph)
+            {
+                e = cudaGraphLaunch(exec, st);
+            }
+            else
+            {
+                iter(st, 0, stages ? &timer : nullptr);
+                iter(st, 1, stages ? &timer : nullptr);
+                e = cudaGetLastError();
+            }
+            iters += 2;
+        }
+        if (e != cudaSuccess) break;
+        e = cudaMemcpyAsync(&w.h_poll[b & 1], &x.ctrl->finished, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            st);
+        if (e == cudaSuccess) e = cudaEventRecord(poll_ev[b & 1], st);
+        run.poll_bytes += sizeof(unsigned long long);
+        if (e == cudaSuccess && b >= 1)
+        {
+            e = cudaEventSynchronize(poll_ev[(b - 1) & 1]);
+            if (e == cudaSuccess && static_cast<int64_t>(w.h_poll[(b - 1) & 1]) >= total) done = true;
+        }
+        if (!done && iters > bound + 4 * kPairsPerPoll)
+        {
+            cudaStreamSynchronize(st);
+            cudaEventDestroy(poll_ev[0]);
+            cudaEventDestroy(poll_ev[1]);
+            release_graph();
+            return fail(MCRT_ERR_INTERNAL, "streaming render did not finish within its iteration bound");
+        }
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(run.e1, st);
+    if (e == cudaSuccess && graph) e = cudaStreamSynchronize(st);  // before the graph is destroyed
+    cudaEventDestroy(poll_ev[0]);
+    cudaEventDestroy(poll_ev[1]);
+    release_graph();
+    if (e != cudaSuccess) return fail(MCRT_ERR_CUDA, std::string("streaming render: ") + cudaGetErrorString(e));
+    run.waves = iters;
+    run.launches += iters * 5;
+    run.extend_launches = iters;
     return MCRT_OK;
 }
 
@@ -882,117 +1363,28 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
         cleanup();
         return fail(MCRT_ERR_STACK_OVERFLOW, "BVH deeper than the traversal stack");
     }
-    // wave boundaries on pixel boundaries so a pixel's samples resolve together
-    int64_t capacity = p0.path_chunk > 0 ? p0.path_chunk : (int64_t(1) << 22);
-    capacity = std::max<int64_t>(capacity, 64);
-    std::vector<int64_t> table;
-    table.push_back(0);
-    {
-        int64_t pos = 0;
-        int     j = 0;
-        while (pos < total)
-        {
-            int64_t end = std::min(total, pos + capacity);
-            while (j + 1 < num_jobs && jobs[j + 1].path_offset <= end - 1) ++j;
-            // job containing `end` (exclusive bound): round down to its pixel boundary
-            int jj = j;
-            while (jj + 1 < num_jobs && jobs[jj + 1].path_offset <= end) ++jj;
-            if (end < total)
-            {
-                int64_t local = end - jobs[jj].path_offset;
-                int64_t rounded = jobs[jj].path_offset + (local / pix_spp[jj]) * pix_spp[jj];
-                if (rounded <= pos)
-                {
-                    // one pixel larger than the capacity: extend to its end
-                    rounded = jobs[jj].path_offset + ((local + pix_spp[jj] - 1) / pix_spp[jj]) * pix_spp[jj];
-                }
-                end = rounded;
-            }
-            table.push_back(end);
-            pos = end;
-        }
-    }
-    int64_t num_chunks = static_cast<int64_t>(table.size()) - 1;
-    int64_t max_chunk = 0;
-    for (int64_t k = 0; k < num_chunks; ++k) max_chunk = std::max(max_chunk, table[k + 1] - table[k]);
-    Workspace& w = owner->ws;
-    int        rc = ensure_workspace(w, max_chunk, num_jobs, num_chunks);
-    if (rc)
-    {
-        cleanup();
-        return rc;
-    }
-    w.args.num_jobs = num_jobs;
-    CK(cudaMemcpyAsync(w.jobs, jobs.data(), sizeof(JobGPU) * num_jobs, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(w.chunk_table, table.data(), sizeof(int64_t) * table.size(), cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(w.ctrl, 0, sizeof(Ctrl), st));
-    CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
-    CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
-
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
-    CK(cudaEventRecord(e0, st));
-    int        launches = 0;
     const bool count = (p0.profile & MCRT_PROFILE_COUNT) != 0;
     const bool stages = (p0.profile & MCRT_PROFILE_STAGES) != 0;
-    StageTimer timer;
+    const bool graph = p0.use_graph && !stages;
     // variant 0: the default policy (32-entry stacks when the tree is shallow enough,
     // registers capped for 8 blocks per SM); MCRT_VARIANT_EXPLICIT: the given bits
-    const int  vb = (p0.variant & MCRT_VARIANT_EXPLICIT) ? p0.variant : (MCRT_VARIANT_STACK32 | MCRT_VARIANT_REGCAP);
-    const bool stack32 = (vb & MCRT_VARIANT_STACK32) && bvh_depth + 2 < 32;
-    const bool regcap = (vb & MCRT_VARIANT_REGCAP) != 0;
+    const int   vb = (p0.variant & MCRT_VARIANT_EXPLICIT) ? p0.variant : (MCRT_VARIANT_STACK32 | MCRT_VARIANT_REGCAP);
+    const bool  stack32 = (vb & MCRT_VARIANT_STACK32) && bvh_depth + 2 < 32;
+    const bool  regcap = (vb & MCRT_VARIANT_REGCAP) != 0;
     LaunchShape lsv = launch_shape_variant(stack32, regcap);
-    auto        enqueue = [&](cudaStream_t s2, StageTimer* tm) {
-        if (stack32)
-        {
-            if (regcap)
-                count ? enqueue_wave<32, true, 8>(w.args, max_depth, lsv, s2, tm)
-                      : enqueue_wave<32, false, 8>(w.args, max_depth, lsv, s2, tm);
-            else
-                count ? enqueue_wave<32, true, 1>(w.args, max_depth, lsv, s2, tm)
-                      : enqueue_wave<32, false, 1>(w.args, max_depth, lsv, s2, tm);
-        }
-        else
-        {
-            if (regcap)
-                count ? enqueue_wave<kStack, true, 8>(w.args, max_depth, lsv, s2, tm)
-                      : enqueue_wave<kStack, false, 8>(w.args, max_depth, lsv, s2, tm);
-            else
-                count ? enqueue_wave<kStack, true, 1>(w.args, max_depth, lsv, s2, tm)
-                      : enqueue_wave<kStack, false, 1>(w.args, max_depth, lsv, s2, tm);
-        }
-    };
-    if (p0.use_graph && !stages)
+    Workspace&  w = owner->ws;
+    StageTimer  timer;
+    RunResult   run;
+    int         rc = p0.schedule == MCRT_SCHEDULE_WAVES
+                         ? run_waves(w, jobs, pix_spp, total, max_depth, p0.path_chunk, stack32, regcap, count, stages,
+                                     graph, lsv, st, timer, run)
+                         : run_stream(w, jobs, pix_spp, total, max_depth, p0.path_chunk, stack32, regcap, count,
+                                      stages, graph, lsv, st, timer, run);
+    if (rc)
     {
-        cudaGraph_t     graph;
-        cudaGraphExec_t exec;
-        cudaStream_t    cap;
-        CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-        CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        enqueue(cap, nullptr);
-        CK(cudaStreamEndCapture(cap, &graph));
-        CK(cudaGraphInstantiate(&exec, graph, 0));
-        for (int64_t k = 0; k < num_chunks; ++k)
-        {
-            CK(cudaGraphLaunch(exec, st));
-            launches += 3 + 3 * (max_depth + 1);
-        }
-        CK(cudaEventRecord(e1, st));
-        CK(cudaStreamSynchronize(st));
-        cudaGraphExecDestroy(exec);
-        cudaGraphDestroy(graph);
-        cudaStreamDestroy(cap);
-    }
-    else
-    {
-        for (int64_t k = 0; k < num_chunks; ++k)
-        {
-            enqueue(st, stages ? &timer : nullptr);
-            launches += 3 + 3 * (max_depth + 1);
-        }
-        CK(cudaGetLastError());
-        CK(cudaEventRecord(e1, st));
+        cudaStreamSynchronize(st);
+        cleanup();
+        return rc;
     }
     if (ptr_mode != MCRT_PTR_DEVICE)
     {
@@ -1006,9 +1398,9 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     CK(cudaMemcpyAsync(&herr, w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    cudaEventElapsedTime(&ms, run.e0, run.e1);
+    cudaEventDestroy(run.e0);
+    cudaEventDestroy(run.e1);
     float stage_ms[4] = {0.f, 0.f, 0.f, 0.f};
     timer.sum(stage_ms);
     cleanup();
@@ -1017,19 +1409,19 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
         stats->paths = total;
         stats->extension_rays = static_cast<int64_t>(hstats[0]);
         stats->shadow_rays = static_cast<int64_t>(hstats[1]);
-        stats->waves = static_cast<int32_t>(num_chunks);
-        stats->kernel_launches = launches;
+        stats->waves = static_cast<int32_t>(run.waves);
+        stats->kernel_launches = static_cast<int32_t>(run.launches);
         stats->device_ms = ms;
         for (int k = 0; k < 4; ++k) stats->stage_ms[k] = stage_ms[k];
-        stats->extend_launches = static_cast<int32_t>(num_chunks * (max_depth + 1));
+        stats->extend_launches = static_cast<int32_t>(run.extend_launches);
         stats->ext_nodes = static_cast<int64_t>(hstats[2]);
         stats->ext_tris = static_cast<int64_t>(hstats[3]);
         stats->nee_nodes = static_cast<int64_t>(hstats[4]);
         stats->nee_tris = static_cast<int64_t>(hstats[5]);
         int64_t img_bytes = 0;
         for (int j = 0; j < num_jobs; ++j) img_bytes += 12 * static_cast<int64_t>(cams[j].width) * cams[j].height;
-        stats->h2d_bytes = static_cast<int64_t>(sizeof(JobGPU)) * num_jobs + 8 * static_cast<int64_t>(table.size());
-        stats->d2h_bytes = static_cast<int64_t>(sizeof(hstats) + sizeof(herr)) +
+        stats->h2d_bytes = static_cast<int64_t>(sizeof(JobGPU)) * num_jobs + run.table_bytes;
+        stats->d2h_bytes = static_cast<int64_t>(sizeof(hstats) + sizeof(herr)) + run.poll_bytes +
                            (ptr_mode != MCRT_PTR_DEVICE ? img_bytes : 0);
     }
     if (herr & kErrStack) return fail(MCRT_ERR_STACK_OVERFLOW, "traversal stack overflow");

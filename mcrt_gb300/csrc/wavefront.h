@@ -54,6 +54,41 @@ struct WaveArgs
     int*                err;
 };
 
+// queues one k_shade launch reads and appends to (counts live in device memory)
+struct QueueSel
+{
+    const int* count;       // rays in the input queue
+    int        qs;          // input ray queue; continuing rays go to queue qs ^ 1
+    int*       next_count;  // append counter of queue qs ^ 1
+    int*       scount;      // [2] append counters of the next-event queues (any-hit, closest-hit)
+    int*       dead_count;  // streaming: append counter of the list of slots whose path ended
+    int*       dead;        //   and the list (nullptr for waves)
+    int        depth;       // waves: the vertex index of every queued path; streaming: -1
+                            // (each slot keeps its own in bits 8.. of thr.w)
+};
+
+// streaming schedule: counters of one render (iteration parity selects the queue pair)
+struct StreamCtrl
+{
+    int                qcount[2];  // ray queues
+    int                dcount[2];  // lists of slots whose path ended
+    int                scount[2];  // next-event queues of the current iteration
+    int                pad[2];
+    unsigned long long next;       // index of the next path to start
+    unsigned long long finished;   // paths whose radiance is in the ring
+};
+
+struct StreamArgs
+{
+    StreamCtrl* ctrl;
+    int*        dead[2];    // slot lists by iteration parity
+    int64_t*    gid;        // path index held by each slot, -1: none
+    float4*     ring;       // radiance of path g at g % ring_size (until its pixel resolves)
+    int*        ring_cnt;   // per pixel, at its first path's ring index: paths finished
+    int64_t     ring_size;
+    int64_t     total;      // paths of the render
+};
+
 struct LaunchShape
 {
     int grid_trace, grid_shade, grid_small, block;

@@ -200,9 +200,9 @@ class GpuScene:
     # -- rayTrace + DemoSimple::run -----------------------------------------------------
     def render(self, camera: CameraDesc, spp: int, max_depth: int, rr_depth: int = -1, seed: int = 0,
                traverse: int = N.TRAVERSE_FAST, out=None, path_chunk: int = 0, use_graph: bool = False,
-               profile: int = 0, variant: int = 0):
+               profile: int = 0, variant: int = 0, schedule: int = N.SCHEDULE_STREAM):
         """Returns (image (H, W, 3) float32, stats dict).  `out` may be a CUDA tensor."""
-        p = make_params(spp, max_depth, rr_depth, seed, traverse, path_chunk, use_graph, profile, variant)
+        p = make_params(spp, max_depth, rr_depth, seed, traverse, path_chunk, use_graph, profile, variant, schedule)
         cam = camera.to_c()
         st = N.RenderStats()
         if out is not None and _is_torch(out):
@@ -254,7 +254,7 @@ class GpuScene:
 
 
 def make_params(spp, max_depth, rr_depth=-1, seed=0, traverse=N.TRAVERSE_FAST, path_chunk=0, use_graph=False,
-                profile=0, variant=0):
+                profile=0, variant=0, schedule=0):
     p = N.RenderParams()
     p.spp = int(spp)
     p.max_depth = int(max_depth)
@@ -265,6 +265,7 @@ def make_params(spp, max_depth, rr_depth=-1, seed=0, traverse=N.TRAVERSE_FAST, p
     p.use_graph = 1 if use_graph else 0
     p.profile = int(profile)
     p.variant = int(variant)
+    p.schedule = int(schedule)
     return p
 
 

@@ -60,15 +60,59 @@ def test_cfg0_ztest_vs_fp64_oracle(cuda_device):
         assert rel < 0.01, f"channel {c}: mean relative error {rel:.4f}"
 
 
-def test_graph_and_stream_paths_agree(cuda_device):
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_graph_and_direct_launches_agree(schedule, cuda_device):
     from mcrt_gb300 import GpuScene
     desc, cam = _cfg0(32)
     sc = GpuScene(desc)
-    a, sa = sc.render(cam, spp=8, max_depth=8, rr_depth=3, seed=5, use_graph=False, path_chunk=3000)
-    b, sb = sc.render(cam, spp=8, max_depth=8, rr_depth=3, seed=5, use_graph=True, path_chunk=3000)
+    kw = dict(spp=8, max_depth=8, rr_depth=3, seed=5, path_chunk=3000, schedule=schedule)
+    a, sa = sc.render(cam, use_graph=False, **kw)
+    b, sb = sc.render(cam, use_graph=True, **kw)
     assert sa["waves"] > 1
-    np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
+    np.testing.assert_array_equal(a, b)
     assert sa["rays"] == sb["rays"]
+
+
+@pytest.mark.parametrize("path_chunk", [64, 256, 3000, 0])
+def test_streaming_equals_waves_bit_exactly(path_chunk, cuda_device):
+    """Path regeneration changes which slot and iteration a path runs in, never its
+    arithmetic: the images are identical.  Small slot counts make the per-path ring wrap
+    (ring = (max_depth + 2) * slots + spp < paths)."""
+    from mcrt_gb300 import GpuScene
+    desc, cam = _cfg0(32)
+    sc = GpuScene(desc)
+    kw = dict(spp=4, max_depth=8, rr_depth=3, seed=13, path_chunk=path_chunk)
+    w, sw = sc.render(cam, schedule=1, **kw)
+    s, ss = sc.render(cam, schedule=0, use_graph=True, **kw)
+    np.testing.assert_array_equal(s, w)
+    assert ss["rays"] == sw["rays"] and ss["paths"] == sw["paths"] == 32 * 32 * 4
+    if path_chunk:
+        assert ss["waves"] > 8
+
+
+def test_streaming_batch_of_uneven_jobs_equals_waves(cuda_device):
+    """Jobs of different spp / depth in one streaming render: each pixel resolves from
+    its own job's samples."""
+    from mcrt_gb300 import GpuScene, render_batch, scenes
+    jobs = scenes.cfg2_jobs(n_scenes=4, seed=5, max_level=4)
+    gs = [GpuScene(d) for d, _, _ in jobs]
+    cams = [c for _, c, _ in jobs]
+    for k, c in enumerate(cams):
+        c.width, c.height = 24 + 8 * k, 16 + 4 * k
+    params = [dict(p, spp=1 + 3 * k, path_chunk=512) for k, (_, _, p) in enumerate(jobs)]
+    outs_s, st_s = render_batch(gs, cams, [dict(p, schedule=0) for p in params])
+    outs_w, st_w = render_batch(gs, cams, [dict(p, schedule=1) for p in params])
+    for a, b in zip(outs_s, outs_w):
+        np.testing.assert_array_equal(a, b)
+    assert st_s["rays"] == st_w["rays"]
+
+
+def test_unknown_schedule_is_rejected(cuda_device):
+    from mcrt_gb300 import GpuScene
+    desc, cam = _cfg0(8)
+    from mcrt_gb300._native import McrtError
+    with pytest.raises(McrtError, match="schedule"):
+        GpuScene(desc).render(cam, spp=1, max_depth=2, schedule=7)
 
 
 def test_batch_equals_individual_renders(cuda_device):
@@ -85,15 +129,17 @@ def test_batch_equals_individual_renders(cuda_device):
         np.testing.assert_allclose(o, single, rtol=1e-5, atol=1e-6)
 
 
-def test_chunking_is_invisible(cuda_device):
-    """Waves of any size give the same image (chunks end on pixel boundaries)."""
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_chunking_is_invisible(schedule, cuda_device):
+    """Waves or slot pools of any size give the same image (waves end on pixel
+    boundaries; streamed pixels resolve from the ring in sample order)."""
     from mcrt_gb300 import GpuScene
     desc, cam = _cfg0(20)
     sc = GpuScene(desc)
-    a, _ = sc.render(cam, spp=5, max_depth=8, rr_depth=3, seed=9, path_chunk=0)
-    b, sb = sc.render(cam, spp=5, max_depth=8, rr_depth=3, seed=9, path_chunk=777)
+    a, _ = sc.render(cam, spp=5, max_depth=8, rr_depth=3, seed=9, path_chunk=0, schedule=schedule)
+    b, sb = sc.render(cam, spp=5, max_depth=8, rr_depth=3, seed=9, path_chunk=777, schedule=schedule)
     assert sb["waves"] > 2
-    np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
+    np.testing.assert_array_equal(a, b)
 
 
 def test_render_into_device_tensor(cuda_device):
