@@ -235,7 +235,7 @@ int mcrt_render_batch(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_ca
  * application's own memory pool, callers under a fixed memory budget.  Same result as
  * mcrt_render with ptr_mode = MCRT_PTR_DEVICE; rgb_out must be device memory.  It always
  * runs the WAVES schedule (params->schedule and params->path_chunk are not used).
- * Scratch: one fixed file-scope device array of about 31 MB, held by every GPU that loads
+ * Scratch: one fixed file-scope device array of about 50 MB, held by every GPU that loads
  * the library's module until the process exits; at most 65,536 path slots per wave
  * (spp <= 65,536) and 65,536 waves per call, larger requests fail with
  * MCRT_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's device

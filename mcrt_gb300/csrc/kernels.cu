@@ -2,18 +2,19 @@
 //
 // Kernels:
 //   k_trace<ANY, MODE>   batch closest/any-hit queries (SceneBVH::intersect / occluded)
-//   wavefront, one set of launches per wave of paths (all graph-capturable: every
-//   count is read from device memory, grids are fixed):
-//     k_begin_chunk      load the wave's path range from the chunk table
-//     k_raygen           camera rays with the tent filter (demo_pt.cpp:689-700)
-//     k_extend           closest hit of the live-path queue
+//   wavefront iterations (wavefront.h; all graph-capturable: every count is read from
+//   device memory, grids are fixed):
+//     k_render_begin, k_wave_next, k_iter_begin   counters and admission
+//     k_regen            finish ended paths (ring, in-order pixel resolve) and start
+//                        camera paths with the tent filter (demo_pt.cpp:689-708)
+//     k_extend           closest hit of the ray queue
 //     k_shade            one vertex of rayTrace (demo_pt.cpp:523-651): emission, NEE with
 //                        MIS against the environment and the area lights, continuation,
-//                        Russian roulette; live paths and shadow rays are appended to
-//                        SoA queues by warp ballot / warp prefix sum + one atomic per warp
-//     k_connect          shadow rays: any hit (environment) or bounded closest hit (area
-//                        lights, which must hit the sampled emitter), MIS-weighted add
-//     k_resolve          per-pixel mean of the clamped per-sample radiance
+//                        Russian roulette; continuing paths, ended paths and next-event
+//                        rays are appended to SoA queues by warp ballot / warp prefix sum
+//                        + one atomic per warp
+//     k_connect          next-event rays: any hit (environment) or bounded closest hit
+//                        (area lights, which must hit the sampled emitter), MIS-weighted
 //   k_adjoint            path-replay adjoint (one thread per path, replayed from its seed)
 #include <cuda_runtime.h>
 
@@ -59,7 +60,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(SceneView s, const float4
 }
 
 // ---------------------------------------------------------------------------
-// wavefront state
+// wavefront stages (the iteration is described in wavefront.h)
 // ---------------------------------------------------------------------------
 // warp-reduced add of per-thread work counters into stats[slot], stats[slot + 1]
 __device__ __forceinline__ void flush_count(unsigned long long* stats, int slot, const TraceCount& c)
@@ -91,97 +92,6 @@ __device__ __forceinline__ int find_job(const JobGPU* jobs, int num_jobs, int64_
     return lo;
 }
 
-__global__ void k_begin_chunk(WaveArgs a)
-{
-    Ctrl* c = a.ctrl;
-    int   idx = c->chunk;
-    c->base = a.chunk_table[idx];
-    c->count = static_cast<int>(a.chunk_table[idx + 1] - a.chunk_table[idx]);
-    c->qcount[0] = c->count;
-    for (int d = 1; d < kMaxDepth + 2; ++d) c->qcount[d] = 0;
-    for (int d = 0; d < kMaxDepth + 1; ++d) c->scount[d][0] = c->scount[d][1] = 0;
-    c->chunk = idx + 1;
-}
-
-// starts camera path g (sample s of pixel x, y of its job) in path slot `slot` and puts
-// its primary ray at position `pos` of ray queue `qsel` (demo_pt.cpp:689-700)
-__device__ __forceinline__ void start_camera_path(const WaveArgs& a, int64_t g, int slot, int qsel, int pos)
-{
-    int           j = find_job(a.jobs, a.num_jobs, g);
-    const JobGPU& J = a.jobs[j];
-    int64_t       local = g - J.path_offset;
-    int           pixel = static_cast<int>(local / J.spp);
-    int           s = static_cast<int>(local - static_cast<int64_t>(pixel) * J.spp);
-    int           x = pixel % J.width, y = pixel / J.width;
-    Pcg           rng;
-    rng.seed(J.seed, static_cast<uint32_t>(pixel), static_cast<uint32_t>(s));
-    float r1 = 2.f * rng.uniform();
-    float r2 = 2.f * rng.uniform();
-    float dx = 0.f, dy = 0.f;
-    if (J.spp > 1)
-    {
-        dx = tent(r1);
-        dy = tent(r2);
-    }
-    float3 o, d;
-    camera_ray(J.cam, (static_cast<float>(x) + 0.5f + dx) / static_cast<float>(J.width),
-               (static_cast<float>(y) + 0.5f + dy) / static_cast<float>(J.height), o, d);
-    a.qo[qsel][pos] = make_float4(o.x, o.y, o.z, kEpsRay);
-    a.qd[qsel][pos] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
-    a.qp[qsel][pos] = slot;
-    a.thr[slot] = make_float4(1.f, 1.f, 1.f, __int_as_float(0));  // flags 0, vertex 0
-    a.rad[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-    a.rng[slot] = rng.state;
-    a.pix[slot] = pixel;
-    a.job[slot] = j;
-    a.pend[slot] = 0;
-}
-
-__global__ void k_raygen(WaveArgs a)
-{
-    const int     count = a.ctrl->count;
-    const int64_t base = a.ctrl->base;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x)
-        start_camera_path(a, base + p, p, 0, p);
-}
-
-// adds a path's pending next-event results in slot order (deterministic sum)
-__device__ __forceinline__ float4 add_pending(const WaveArgs& a, int p, float4 r)
-{
-    int m = a.pend[p];
-    for (int s = 0; s < 4; ++s)
-        if (m & (1 << s))
-        {
-            float4 v = a.nee_val[4 * p + s];
-            r.x += v.x;
-            r.y += v.y;
-            r.z += v.z;
-        }
-    return r;
-}
-
-template <int STACK, bool COUNT, int MINB>
-__global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, const int* count, int qs)
-{
-    __shared__ int stack[STACK * kTraceBlock];
-    int*           st = stack + threadIdx.x;
-    const int      n = min(*count, static_cast<int>(a.capacity));
-    TraceCount     cnt = {0u, 0u};
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[0], static_cast<unsigned long long>(n));
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    {
-        float4 o = a.qo[qs][i], d = a.qd[qs][i];
-        int    p = a.qp[qs][i];
-        int    j = a.job[p];
-        Hit    h;
-        bool   hit = trace_ray<false, STACK, COUNT>(a.jobs[j].scene, a.jobs[j].traverse, xyz(o), xyz(d), o.w, d.w,
-                                                  st, kTraceBlock, h, a.err, &cnt);
-        a.hits[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.prim))
-                        : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
-    }
-    if (COUNT) flush_count(a.stats, 2, cnt);
-}
-
 __device__ __forceinline__ unsigned lanemask_lt()
 {
     unsigned m;
@@ -207,37 +117,251 @@ __device__ __forceinline__ int warp_append(int* counter, int k)
     return base + incl - k;
 }
 
-__global__ void __launch_bounds__(128) k_shade(WaveArgs a, QueueSel q)
+// adds a path's pending next-event results (slots[0..3], bits of `mask`) in slot order:
+// the order in which rayTrace adds them (deterministic sum)
+__device__ __forceinline__ float4 add_pending(const float4* slots, int mask, float4 r)
 {
-    const int n = min(*q.count, static_cast<int>(a.capacity));
-    const int qs = q.qs;
-    const int lane = threadIdx.x & 31;
-    const int warps_total = (gridDim.x * blockDim.x) >> 5;
+    for (int s = 0; s < 4; ++s)
+        if (mask & (1 << s))
+        {
+            float4 v = slots[s];
+            r.x += v.x;
+            r.y += v.y;
+            r.z += v.z;
+        }
+    return r;
+}
+
+// counters of a new render; the wave schedule admits nothing until k_wave_next
+__global__ void k_render_begin(WaveArgs a, int waves, int64_t limit)
+{
+    Ctrl* c = a.ctrl;
+    c->qcount[0] = c->qcount[1] = 0;
+    c->dcount[0] = c->dcount[1] = 0;
+    c->scount[0] = c->scount[1] = 0;
+    c->new_base = c->new_count = 0;
+    c->chunk = -1;
+    c->pad = 0;
+    c->next = 0;
+    c->limit = waves ? 0ull : static_cast<unsigned long long>(limit);
+    c->new_g = 0;
+    c->finished = 0;
+}
+
+// wave schedule: admit the next wave's paths
+__global__ void k_wave_next(WaveArgs a)
+{
+    Ctrl* c = a.ctrl;
+    c->chunk += 1;
+    c->limit = static_cast<unsigned long long>(a.chunk_table[c->chunk + 1]);
+}
+
+__global__ void k_iter_begin(WaveArgs a, int p)
+{
+    Ctrl* c = a.ctrl;
+    c->qcount[p ^ 1] = 0;
+    c->dcount[p ^ 1] = 0;
+    c->scount[0] = 0;
+    c->scount[1] = 0;
+    // top the queue up with new paths (continuing rays are already in it)
+    const int                q = c->qcount[p];
+    const unsigned long long avail = c->limit > c->next ? c->limit - c->next : 0ull;
+    const long long          room = a.capacity - static_cast<long long>(q);
+    const int n = room > 0 ? static_cast<int>(avail < static_cast<unsigned long long>(room) ? avail : room) : 0;
+    c->new_base = q;
+    c->new_count = n;
+    c->new_g = c->next;
+    c->qcount[p] = q + n;
+    c->next += static_cast<unsigned long long>(n);
+}
+
+// starts camera path g (sample s of pixel x, y of its job) at position `pos` of ray
+// queue p (demo_pt.cpp:689-700)
+__device__ __forceinline__ void start_camera_path(const WaveArgs& a, int64_t g, int p, int pos)
+{
+    int           j = find_job(a.jobs, a.num_jobs, g);
+    const JobGPU& J = a.jobs[j];
+    int64_t       local = g - J.path_offset;
+    int           pixel = static_cast<int>(local / J.spp);
+    int           s = static_cast<int>(local - static_cast<int64_t>(pixel) * J.spp);
+    int           x = pixel % J.width, y = pixel / J.width;
+    Pcg           rng;
+    rng.seed(J.seed, static_cast<uint32_t>(pixel), static_cast<uint32_t>(s));
+    float r1 = 2.f * rng.uniform();
+    float r2 = 2.f * rng.uniform();
+    float dx = 0.f, dy = 0.f;
+    if (J.spp > 1)
+    {
+        dx = tent(r1);
+        dy = tent(r2);
+    }
+    float3 o, d;
+    camera_ray(J.cam, (static_cast<float>(x) + 0.5f + dx) / static_cast<float>(J.width),
+               (static_cast<float>(y) + 0.5f + dy) / static_cast<float>(J.height), o, d);
+    a.qo[p][pos] = make_float4(o.x, o.y, o.z, __int_as_float(j));
+    a.qd[p][pos] = make_float4(d.x, d.y, d.z, __int_as_float(pixel));
+    a.qthr[p][pos] = make_float4(1.f, 1.f, 1.f, __int_as_float(0));  // vertex 0, nothing pending
+    a.qrad[p][pos] = make_float4(0.f, 0.f, 0.f, __int_as_float(s));
+    a.qrng[p][pos] = rng.state;
+}
+
+// Finishes the warp's ended paths (lanes with `valid`): radiance into the ring; a pixel
+// whose last path this was is resolved by the whole warp from the ring in sample order,
+// with the arithmetic of FrameBuffer::accumulatePixel / scale.  Called by all 32 lanes.
+__device__ __forceinline__ void finish_paths(const WaveArgs& a, int p, int i, bool valid, unsigned long long& fin)
+{
+    const int     lane = threadIdx.x & 31;
+    const int64_t R = a.ring_size;
+    int64_t       cidx = 0;
+    int           spp = 0, pixel = 0, job = 0;
+    if (valid)
+    {
+        const int4    m = a.dmeta[p][i];
+        const float4 r = add_pending(a.nev[p] + 4 * a.capacity + 4 * static_cast<int64_t>(i), m.z, a.drad[p][i]);
+        pixel = m.x;
+        job = m.y;
+        const JobGPU& J = a.jobs[job];
+        const int64_t first = J.path_offset + static_cast<int64_t>(pixel) * J.spp;
+        a.ring[(first + __float_as_int(r.w)) % R] = make_float4(r.x, r.y, r.z, 0.f);
+        cidx = first % R;
+        spp = J.spp;
+        ++fin;
+    }
+    __threadfence();  // ring entries visible before the counts that announce them
+    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+    bool           resolve = false;
+    if (valid)
+    {
+        // lanes finishing paths of the same pixel add to its count once
+        const unsigned peers = __match_any_sync(vmask, static_cast<unsigned long long>(cidx));
+        if (lane == __ffs(peers) - 1)
+        {
+            const int k = __popc(peers);
+            resolve = atomicAdd(&a.ring_cnt[cidx], k) + k == spp;
+        }
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, resolve);
+    if (!todo) return;
+    __threadfence();
+    while (todo)
+    {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int64_t c0 = __shfl_sync(0xffffffffu, cidx, src);
+        const int     sp = __shfl_sync(0xffffffffu, spp, src);
+        const int     px = __shfl_sync(0xffffffffu, pixel, src);
+        const int     jb = __shfl_sync(0xffffffffu, job, src);
+        float         s0 = 0.f, s1 = 0.f, s2 = 0.f;
+        for (int k0 = 0; k0 < sp; k0 += 32)
+        {
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k0 + lane < sp)
+            {
+                int64_t idx = c0 + k0 + lane;
+                if (idx >= R) idx -= R;
+                v = __ldcg(&a.ring[idx]);  // L2: written by other blocks of this launch
+                if (isnan3(xyz(v))) v = make_float4(0.f, 0.f, 0.f, 0.f);  // demo_pt.cpp:653
+                v.x = fmax_ref(0.f, v.x);                                   // demo_pt.cpp:703
+                v.y = fmax_ref(0.f, v.y);
+                v.z = fmax_ref(0.f, v.z);
+            }
+            const int m = min(32, sp - k0);
+            for (int l = 0; l < m; ++l)  // sample order
+            {
+                s0 += __shfl_sync(0xffffffffu, v.x, l);
+                s1 += __shfl_sync(0xffffffffu, v.y, l);
+                s2 += __shfl_sync(0xffffffffu, v.z, l);
+            }
+        }
+        if (lane == 0)
+        {
+            a.ring_cnt[c0] = 0;
+            const JobGPU& J = a.jobs[jb];
+            const float   scale = static_cast<float>(1.0 / J.spp);  // FrameBuffer::scale(1.0 / spp)
+            float*        out = J.image + 3 * static_cast<int64_t>(px);
+            out[0] = s0 * scale;
+            out[1] = s1 * scale;
+            out[2] = s2 * scale;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_regen(WaveArgs a, int p)
+{
+    const Ctrl*        c = a.ctrl;
+    const int          nd = min(c->dcount[p], static_cast<int>(a.capacity));
+    const int          nn = c->new_count;
+    const int          nb = c->new_base;
+    const int64_t      g0 = static_cast<int64_t>(c->new_g);
+    const int          n = max(nd, nn);
+    const int          lane = threadIdx.x & 31;
+    const int          warps_total = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long fin = 0;
     for (int wbase = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < n; wbase += warps_total * 32)
     {
-        int  i = wbase + lane;
-        bool valid = i < n;
+        const int i = wbase + lane;
+        if (wbase < nd) finish_paths(a, p, i, i < nd, fin);
+        if (i < nn) start_camera_path(a, g0 + i, p, nb + i);
+    }
+    for (int off = 16; off > 0; off >>= 1) fin += __shfl_down_sync(0xffffffffu, fin, off);
+    if (lane == 0 && fin) atomicAdd(&a.ctrl->finished, fin);
+}
+
+template <int STACK, bool COUNT, int MINB>
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
+{
+    __shared__ int stack[STACK * kTraceBlock];
+    int*           st = stack + threadIdx.x;
+    const int      n = min(a.ctrl->qcount[p], static_cast<int>(a.capacity));
+    TraceCount     cnt = {0u, 0u};
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[0], static_cast<unsigned long long>(n));
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        float4        o = a.qo[p][i], d = a.qd[p][i];
+        const JobGPU& J = a.jobs[__float_as_int(o.w)];
+        Hit           h;
+        bool hit = trace_ray<false, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), kEpsRay,
+                                                  __int_as_float(0x7f800000), st, kTraceBlock, h, a.err, &cnt);
+        a.hits[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.prim))
+                        : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    }
+    if (COUNT) flush_count(a.stats, 2, cnt);
+}
+
+__global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
+{
+    const int n = min(a.ctrl->qcount[p], static_cast<int>(a.capacity));
+    const int lane = threadIdx.x & 31;
+    const int warps_total = (gridDim.x * blockDim.x) >> 5;
+    const int pn = p ^ 1;
+    for (int wbase = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < n; wbase += warps_total * 32)
+    {
+        int      i = wbase + lane;
+        bool     valid = i < n;
         bool     cont = false;
         float3   phit = mk(0.f, 0.f, 0.f), cdir = mk(0.f, 0.f, 1.f), T2 = mk(0.f, 0.f, 0.f);
-        int      flags2 = 0, n_nee = 0, p = 0, depth = 0;
+        float4   rnew = make_float4(0.f, 0.f, 0.f, 0.f);
+        int      flags2 = 0, n_nee = 0, job = 0, pixel = 0;
         uint64_t rstate = 0;
         NeeRay   nee[4];
         if (valid)
         {
-            float4           o4 = a.qo[qs][i], d4 = a.qd[qs][i];
+            float4           o4 = a.qo[p][i], d4 = a.qd[p][i];
             float4           hh = a.hits[i];
+            float4           t4 = a.qthr[p][i];
             float3           o = xyz(o4), d = xyz(d4);
-            p = a.qp[qs][i];
-            const JobGPU&    J = a.jobs[a.job[p]];
+            job = __float_as_int(o4.w);
+            pixel = __float_as_int(d4.w);
+            const JobGPU&    J = a.jobs[job];
             const SceneView& S = J.scene;
-            float4           t4 = a.thr[p];
             float3           T = xyz(t4);
-            depth = q.depth >= 0 ? q.depth : (__float_as_int(t4.w) >> 8);
-            bool             no_direct = depth == 0 || !(__float_as_int(t4.w) & 1);
+            const int        flags = __float_as_int(t4.w);
+            const int        depth = (flags >> 8) & 0xff;
+            bool             no_direct = depth == 0 || !(flags & 1);
             int              prim = __float_as_int(hh.w);
             float3           Ladd = mk(0.f, 0.f, 0.f);
             // results of the previous vertex's next-event rays first, then this vertex
-            float4 rp = add_pending(a, p, a.rad[p]);
+            float4 rp = add_pending(a.nev[p] + 4 * static_cast<int64_t>(i), (flags >> 16) & 0xf, a.qrad[p][i]);
             if (prim < 0)
             {
                 Ladd = miss_emission(S, d, T, no_direct);
@@ -255,8 +379,8 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, QueueSel q)
                 else
                 {
                     Pcg rng;
-                    rng.state = a.rng[p];
-                    rng.inc = (static_cast<uint64_t>(a.pix[p]) << 1u) | 1u;
+                    rng.state = a.qrng[p][i];
+                    rng.inc = (static_cast<uint64_t>(pixel) << 1u) | 1u;
                     float u[NUM_DIMS];
 #pragma unroll
                     for (int k = 0; k < NUM_DIMS; ++k) u[k] = rng.uniform();
@@ -268,27 +392,29 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, QueueSel q)
                     flags2 = (nee_here ? 1 : 0) | ((depth + 1) << 8);
                 }
             }
-            a.rad[p] = make_float4(rp.x + Ladd.x, rp.y + Ladd.y, rp.z + Ladd.z, rp.w);
-            a.pend[p] = (1 << n_nee) - 1;
+            rnew = make_float4(rp.x + Ladd.x, rp.y + Ladd.y, rp.z + Ladd.z, rp.w);
         }
-        // compaction of live paths into the next queue (ballot + popc, one atomic per warp)
+        const int pend = (1 << n_nee) - 1;
+        // continuing paths -> queue p ^ 1, ended paths -> finished list p ^ 1 (ballot + popc,
+        // one atomic per warp each); dest: where this vertex's next-event results go
+        int      dest = -1;
         unsigned live = __ballot_sync(0xffffffffu, cont);
         if (live)
         {
             int base = 0;
-            if (lane == 0) base = atomicAdd(q.next_count, __popc(live));
+            if (lane == 0) base = atomicAdd(&a.ctrl->qcount[pn], __popc(live));
             base = __shfl_sync(0xffffffffu, base, 0);
             if (cont)
             {
                 int k = base + __popc(live & lanemask_lt());
-                int qn = qs ^ 1;
                 if (k < a.capacity)
                 {
-                    a.qo[qn][k] = make_float4(phit.x, phit.y, phit.z, kEpsRay);
-                    a.qd[qn][k] = make_float4(cdir.x, cdir.y, cdir.z, __int_as_float(0x7f800000));
-                    a.qp[qn][k] = p;
-                    a.thr[p] = make_float4(T2.x, T2.y, T2.z, __int_as_float(flags2));
-                    a.rng[p] = rstate;
+                    a.qo[pn][k] = make_float4(phit.x, phit.y, phit.z, __int_as_float(job));
+                    a.qd[pn][k] = make_float4(cdir.x, cdir.y, cdir.z, __int_as_float(pixel));
+                    a.qthr[pn][k] = make_float4(T2.x, T2.y, T2.z, __int_as_float(flags2 | (pend << 16)));
+                    a.qrad[pn][k] = rnew;
+                    a.qrng[pn][k] = rstate;
+                    dest = 4 * k;
                 }
                 else
                 {
@@ -296,25 +422,28 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, QueueSel q)
                 }
             }
         }
-        // streaming: slots whose path ended are listed for the next iteration's k_regen
-        if (q.dead)
+        unsigned ended = __ballot_sync(0xffffffffu, valid && !cont);
+        if (ended)
         {
-            unsigned fin = __ballot_sync(0xffffffffu, valid && !cont);
-            if (fin)
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&a.ctrl->dcount[pn], __popc(ended));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (valid && !cont)
             {
-                int base = 0;
-                if (lane == 0) base = atomicAdd(q.dead_count, __popc(fin));
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (valid && !cont)
+                int k = base + __popc(ended & lanemask_lt());
+                if (k < a.capacity)
                 {
-                    int k = base + __popc(fin & lanemask_lt());
-                    if (k < a.capacity)
-                        q.dead[k] = p;
-                    else
-                        atomicOr(a.err, kErrQueue);
+                    a.drad[pn][k] = rnew;
+                    a.dmeta[pn][k] = make_int4(pixel, job, pend, 0);
+                    dest = static_cast<int>(4 * a.capacity) + 4 * k;
+                }
+                else
+                {
+                    atomicOr(a.err, kErrQueue);
                 }
             }
         }
+        if (dest < 0) n_nee = 0;  // no place for the results (queue overflow, reported)
         // next-event rays: any-hit queue [0], closest-hit queue [1] (warp prefix sums)
         int n_any = 0;
         for (int r = 0; r < n_nee; ++r) n_any += nee[r].type == NEE_ENV ? 1 : 0;
@@ -322,7 +451,7 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, QueueSel q)
         for (int qsel = 0; qsel < 2; ++qsel)
         {
             int k = qsel == 0 ? n_any : n_cl;
-            int b = warp_append(&q.scount[qsel], k);
+            int b = warp_append(&a.ctrl->scount[qsel], k);
             int w = 0;
             for (int r = 0; r < n_nee; ++r)
             {
@@ -336,20 +465,21 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, QueueSel q)
                 a.so[qsel][idx] = make_float4(phit.x, phit.y, phit.z, kEpsRay);
                 a.sd[qsel][idx] = make_float4(nee[r].d.x, nee[r].d.y, nee[r].d.z, nee[r].tmax);
                 a.sv[qsel][idx] = nee[r].val;
-                a.sm[qsel][idx] = make_int4(p, nee[r].type, nee[r].light, r);
+                a.sm[qsel][idx] = make_int4(dest + r, nee[r].type, nee[r].light, job);
             }
         }
     }
 }
 
 template <int STACK, bool COUNT, int MINB>
-__global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, const int* counts)
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, int p)
 {
     __shared__ int stack[STACK * kTraceBlock];
     int*           st = stack + threadIdx.x;
     TraceCount     cnt = {0u, 0u};
-    const int      n0 = min(counts[0], static_cast<int>(a.shadow_cap));
-    const int      n1 = min(counts[1], static_cast<int>(a.shadow_cap));
+    const int      n0 = min(a.ctrl->scount[0], static_cast<int>(a.shadow_cap));
+    const int      n1 = min(a.ctrl->scount[1], static_cast<int>(a.shadow_cap));
+    float4*        res = a.nev[p ^ 1];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[1], static_cast<unsigned long long>(n0 + n1));
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0 + n1; i += gridDim.x * blockDim.x)
     {
@@ -357,8 +487,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, const
         int              k = i < n0 ? i : i - n0;
         float4           o = a.so[q][k], d = a.sd[q][k], v = a.sv[q][k];
         int4             m = a.sm[q][k];
-        int              p = m.x;
-        const JobGPU&    J = a.jobs[a.job[p]];
+        const JobGPU&    J = a.jobs[m.w];
         const SceneView& S = J.scene;
         Hit              h;
         bool hit = q == 0 ? trace_ray<true, STACK, COUNT>(S, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock, h,
@@ -368,7 +497,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, const
         float3 coef;
         int    emat;
         float3 add = nee_contribution(S, m.y, m.z, v, xyz(d), hit, h, coef, emat);
-        a.nee_val[4 * p + m.w] = make_float4(add.x, add.y, add.z, 0.f);
+        res[m.x] = make_float4(add.x, add.y, add.z, 0.f);
     }
     if (COUNT) flush_count(a.stats, 4, cnt);
 }
@@ -551,143 +680,6 @@ __global__ void __launch_bounds__(kAdjBlock) k_adjoint(AdjointArgs a)
     }
 }
 
-__global__ void k_resolve(WaveArgs a)
-{
-    const int     count = a.ctrl->count;
-    const int64_t base = a.ctrl->base;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x)
-    {
-        int64_t       g = base + p;
-        int           j = find_job(a.jobs, a.num_jobs, g);
-        const JobGPU& J = a.jobs[j];
-        int64_t       local = g - J.path_offset;
-        if (local % J.spp != 0) continue;
-        int   pixel = static_cast<int>(local / J.spp);
-        float s[3] = {0.f, 0.f, 0.f};
-        for (int k = 0; k < J.spp; ++k)
-        {
-            float4 r = add_pending(a, p + k, a.rad[p + k]);
-            if (isnan3(xyz(r))) r = make_float4(0.f, 0.f, 0.f, 0.f);  // demo_pt.cpp:653
-            s[0] += fmax_ref(0.f, r.x);                                // demo_pt.cpp:703
-            s[1] += fmax_ref(0.f, r.y);
-            s[2] += fmax_ref(0.f, r.z);
-        }
-        float scale = static_cast<float>(1.0 / J.spp);  // FrameBuffer::scale(1.0 / spp)
-        float* px = J.image + 3 * static_cast<int64_t>(pixel);
-        px[0] = s[0] * scale;
-        px[1] = s[1] * scale;
-        px[2] = s[2] * scale;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// streaming schedule (path regeneration).  Per iteration, with parity par:
-//   k_stream_begin  zero the counters the iteration appends to
-//   k_regen         slots listed dead[par] (their path ended in the previous iteration's
-//                   k_shade, its next-event results are in): store the path's radiance
-//                   in the ring, resolve its pixel if that was the pixel's last path, and
-//                   start the next camera path in the slot (ray queue par)
-//   k_extend, k_shade, k_connect on ray queue par; k_shade appends continuing rays to
-//                   queue par ^ 1 and the slots of ended paths to dead[par ^ 1]
-// A slot starts at most one path per iteration and a path needs at most max_depth + 2
-// iterations from start to ring, so with C slots the paths whose ring entries are live
-// span fewer than (max_depth + 2) * C + spp indices: a ring of that size never
-// overwrites an entry before its pixel is resolved.
-// ---------------------------------------------------------------------------
-__global__ void k_stream_init(WaveArgs a, StreamArgs s)
-{
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < a.capacity;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    {
-        s.dead[0][i] = static_cast<int>(i);
-        s.gid[i] = -1;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) s.ctrl->dcount[0] = static_cast<int>(a.capacity);
-}
-
-__global__ void k_stream_begin(StreamArgs s, int par)
-{
-    s.ctrl->qcount[par ^ 1] = 0;
-    s.ctrl->dcount[par ^ 1] = 0;
-    s.ctrl->scount[0] = 0;
-    s.ctrl->scount[1] = 0;
-}
-
-// stores the radiance of path g (held by `slot`) in the ring; the call that stores the
-// last path of a pixel resolves the pixel from the ring in sample order, with the
-// arithmetic of k_resolve
-__device__ __forceinline__ void finish_path(const WaveArgs& a, const StreamArgs& s, int slot, int64_t g)
-{
-    float4        r = add_pending(a, slot, a.rad[slot]);
-    const JobGPU& J = a.jobs[a.job[slot]];
-    const int64_t R = s.ring_size;
-    const int     pixel = a.pix[slot];
-    const int64_t first = J.path_offset + static_cast<int64_t>(pixel) * J.spp;
-    s.ring[g % R] = r;
-    __threadfence();  // the entry is visible before the count that announces it
-    const int64_t c = first % R;
-    if (atomicAdd(&s.ring_cnt[c], 1) != J.spp - 1) return;
-    __threadfence();
-    s.ring_cnt[c] = 0;
-    float   acc[3] = {0.f, 0.f, 0.f};
-    int64_t idx = c;
-    for (int k = 0; k < J.spp; ++k)
-    {
-        float4 v = __ldcg(&s.ring[idx]);  // L2: written by other blocks of this launch
-        if (isnan3(xyz(v))) v = make_float4(0.f, 0.f, 0.f, 0.f);  // demo_pt.cpp:653
-        acc[0] += fmax_ref(0.f, v.x);                               // demo_pt.cpp:703
-        acc[1] += fmax_ref(0.f, v.y);
-        acc[2] += fmax_ref(0.f, v.z);
-        if (++idx == R) idx = 0;
-    }
-    float  scale = static_cast<float>(1.0 / J.spp);  // FrameBuffer::scale(1.0 / spp)
-    float* px = J.image + 3 * static_cast<int64_t>(pixel);
-    px[0] = acc[0] * scale;
-    px[1] = acc[1] * scale;
-    px[2] = acc[2] * scale;
-}
-
-__global__ void __launch_bounds__(128) k_regen(WaveArgs a, StreamArgs s, int par)
-{
-    const int          nd = min(s.ctrl->dcount[par], static_cast<int>(a.capacity));
-    const int          lane = threadIdx.x & 31;
-    const int          warps_total = (gridDim.x * blockDim.x) >> 5;
-    unsigned long long fin = 0;
-    for (int wbase = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < nd; wbase += warps_total * 32)
-    {
-        const int  i = wbase + lane;
-        const bool valid = i < nd;
-        const int  slot = valid ? s.dead[par][i] : 0;
-        if (valid)
-        {
-            const int64_t g = s.gid[slot];
-            if (g >= 0)
-            {
-                finish_path(a, s, slot, g);
-                ++fin;
-            }
-        }
-        // the warp's slots take consecutive path indices (neighbouring samples)
-        const unsigned     want = __ballot_sync(0xffffffffu, valid);
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&s.ctrl->next, static_cast<unsigned long long>(__popc(want)));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        const int64_t g = static_cast<int64_t>(base) + __popc(want & lanemask_lt());
-        const bool    start = valid && g < s.total;
-        const int     pos = warp_append(&s.ctrl->qcount[par], start ? 1 : 0);
-        if (valid) s.gid[slot] = start ? g : -1;
-        if (start)
-        {
-            if (pos < a.capacity)
-                start_camera_path(a, g, slot, par, pos);
-            else
-                atomicOr(a.err, kErrQueue);
-        }
-    }
-    for (int off = 16; off > 0; off >>= 1) fin += __shfl_down_sync(0xffffffffu, fin, off);
-    if (lane == 0 && fin) atomicAdd(&s.ctrl->finished, fin);
-}
-
 }  // namespace mcrt
 
 // ===========================================================================
@@ -716,51 +708,30 @@ int fail(int code, const std::string& msg)
 
 struct Workspace
 {
-    int64_t  capacity = 0;
-    int      jobs_cap = 0;
-    int64_t  chunks_cap = 0;
-    WaveArgs args{};
-    void*    block = nullptr;  // one allocation for the per-path arrays
-    JobGPU*  jobs = nullptr;
-    int64_t* chunk_table = nullptr;
-    Ctrl*    ctrl = nullptr;
+    int64_t             capacity = 0;  // rays per queue of `block`
+    int64_t             ring = 0;      // entries of `ring_block`
+    int                 jobs_cap = 0;
+    int64_t             chunks_cap = 0;
+    WaveArgs            args{};
+    void*               block = nullptr;       // queues
+    void*               ring_block = nullptr;  // ring + per-pixel counts
+    JobGPU*             jobs = nullptr;
+    int64_t*            chunk_table = nullptr;
+    Ctrl*               ctrl = nullptr;
     unsigned long long* stats = nullptr;
-    int*     err = nullptr;
-    // streaming schedule
-    int64_t             s_capacity = 0;  // slots of s_block (dead lists, gid)
-    int64_t             s_ring = 0;      // entries of s_ring_block (ring, ring_cnt)
-    void*               s_block = nullptr;
-    void*               s_ring_block = nullptr;
-    StreamCtrl*         s_ctrl = nullptr;
-    unsigned long long* h_poll = nullptr;  // pinned: completion polls
-    StreamArgs          sargs{};
+    int*                err = nullptr;
+    unsigned long long* h_poll = nullptr;  // pinned: completion polls of the streaming schedule
     void release()
     {
-        cudaFree(s_block);
-        cudaFree(s_ring_block);
-        cudaFree(s_ctrl);
-        cudaFreeHost(h_poll);
-        s_block = nullptr;
-        s_ring_block = nullptr;
-        s_ctrl = nullptr;
-        h_poll = nullptr;
-        s_capacity = 0;
-        s_ring = 0;
         cudaFree(block);
+        cudaFree(ring_block);
         cudaFree(jobs);
         cudaFree(chunk_table);
         cudaFree(ctrl);
         cudaFree(stats);
         cudaFree(err);
-        block = nullptr;
-        jobs = nullptr;
-        chunk_table = nullptr;
-        ctrl = nullptr;
-        stats = nullptr;
-        err = nullptr;
-        capacity = 0;
-        jobs_cap = 0;
-        chunks_cap = 0;
+        cudaFreeHost(h_poll);
+        *this = Workspace{};
     }
 };
 
@@ -855,20 +826,30 @@ CameraGPU make_camera_impl(const mcrt_camera& c)
     return g;
 }
 
-int ensure_workspace(Workspace& w, int64_t capacity, int num_jobs, int64_t num_chunks)
+// queues for `capacity` rays, a ring of `ring` entries, `num_jobs` jobs, `num_chunks` waves
+int ensure_workspace(Workspace& w, int64_t capacity, int64_t ring, int num_jobs, int64_t num_chunks)
 {
     if (w.capacity < capacity)
     {
         cudaFree(w.block);
         w.block = nullptr;
-        CK(cudaMalloc(&w.block, wave_bytes(capacity)));
-        carve_wave(w.args, w.block, capacity);
+        w.capacity = 0;
+        CK(cudaMalloc(&w.block, queue_bytes(capacity)));
         w.capacity = capacity;
+    }
+    if (w.ring < ring)
+    {
+        cudaFree(w.ring_block);
+        w.ring_block = nullptr;
+        w.ring = 0;
+        CK(cudaMalloc(&w.ring_block, ring_bytes(ring)));
+        w.ring = ring;
     }
     if (w.jobs_cap < num_jobs)
     {
         cudaFree(w.jobs);
         w.jobs = nullptr;
+        w.jobs_cap = 0;
         CK(cudaMalloc(&w.jobs, sizeof(JobGPU) * num_jobs));
         w.jobs_cap = num_jobs;
     }
@@ -876,6 +857,7 @@ int ensure_workspace(Workspace& w, int64_t capacity, int num_jobs, int64_t num_c
     {
         cudaFree(w.chunk_table);
         w.chunk_table = nullptr;
+        w.chunks_cap = 0;
         CK(cudaMalloc(&w.chunk_table, sizeof(int64_t) * (num_chunks + 1)));
         w.chunks_cap = num_chunks + 1;
     }
@@ -884,7 +866,10 @@ int ensure_workspace(Workspace& w, int64_t capacity, int num_jobs, int64_t num_c
         CK(cudaMalloc(&w.ctrl, sizeof(Ctrl)));
         CK(cudaMalloc(&w.stats, sizeof(unsigned long long) * 8));
         CK(cudaMalloc(&w.err, sizeof(int)));
+        CK(cudaMallocHost(&w.h_poll, 2 * sizeof(unsigned long long)));
     }
+    if (w.block) carve_queues(w.args, w.block, w.capacity);
+    if (w.ring_block) carve_ring(w.args, w.ring_block, w.ring);
     w.args.ctrl = w.ctrl;
     w.args.jobs = w.jobs;
     w.args.chunk_table = w.chunk_table;
@@ -920,8 +905,10 @@ struct StageTimer
     }
 };
 
+// one iteration of parity p (five launches); stage timer slots: 0 begin + regen,
+// 1 extend, 2 shade, 3 connect
 template <int STACK, bool COUNT, int MINB>
-void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st, StageTimer* tm)
+void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, StageTimer* tm)
 {
     auto beg = [&](int stg) {
         if (tm) tm->record(st, stg, true);
@@ -930,53 +917,30 @@ void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaS
         if (tm) tm->record(st, 0, false);
     };
     beg(0);
-    k_begin_chunk<<<1, 1, 0, st>>>(a);
-    k_raygen<<<ls.grid_small, 256, 0, st>>>(a);
+    k_iter_begin<<<1, 1, 0, st>>>(a, p);
+    k_regen<<<ls.grid_shade, 128, 0, st>>>(a, p);
     end();
-    for (int d = 0; d <= max_depth; ++d)
-    {
-        beg(1);
-        k_extend<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, &a.ctrl->qcount[d], d & 1);
-        end();
-        beg(2);
-        QueueSel q{&a.ctrl->qcount[d], d & 1, &a.ctrl->qcount[d + 1], a.ctrl->scount[d], nullptr, nullptr, d};
-        k_shade<<<ls.grid_shade, 128, 0, st>>>(a, q);
-        end();
-        beg(3);
-        k_connect<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, a.ctrl->scount[d]);
-        end();
-    }
-    beg(0);
-    k_resolve<<<ls.grid_small, 256, 0, st>>>(a);
+    beg(1);
+    k_extend<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, p);
+    end();
+    beg(2);
+    k_shade<<<ls.grid_shade, 128, 0, st>>>(a, p);
+    end();
+    beg(3);
+    k_connect<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, p);
     end();
 }
 
-// one streaming iteration of parity `par` (five launches)
+// one wave of the wave schedule: admit the wave, then iterate until its last path is
+// finished (an even count, so the next wave starts on parity 0)
 template <int STACK, bool COUNT, int MINB>
-void enqueue_stream_iter(const WaveArgs& a, const StreamArgs& x, int par, const LaunchShape& ls, cudaStream_t st,
-                         StageTimer* tm)
+void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st, StageTimer* tm)
 {
-    auto beg = [&](int stg) {
-        if (tm) tm->record(st, stg, true);
-    };
-    auto end = [&]() {
-        if (tm) tm->record(st, 0, false);
-    };
-    beg(0);
-    k_stream_begin<<<1, 1, 0, st>>>(x, par);
-    k_regen<<<ls.grid_shade, 128, 0, st>>>(a, x, par);
-    end();
-    beg(1);
-    k_extend<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, &x.ctrl->qcount[par], par);
-    end();
-    beg(2);
-    QueueSel q{&x.ctrl->qcount[par], par, &x.ctrl->qcount[par ^ 1], x.ctrl->scount, &x.ctrl->dcount[par ^ 1],
-               x.dead[par ^ 1], -1};
-    k_shade<<<ls.grid_shade, 128, 0, st>>>(a, q);
-    end();
-    beg(3);
-    k_connect<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, x.ctrl->scount);
-    end();
+    if (tm) tm->record(st, 0, true);
+    k_wave_next<<<1, 1, 0, st>>>(a);
+    if (tm) tm->record(st, 0, false);
+    const int iters = wave_iterations(max_depth);
+    for (int t = 0; t < iters; ++t) enqueue_iter<STACK, COUNT, MINB>(a, t & 1, ls, st, tm);
 }
 
 int validate_job_impl(const mcrt_scene* s, const mcrt_camera* c, const mcrt_render_params* p)
@@ -993,6 +957,8 @@ int validate_job_impl(const mcrt_scene* s, const mcrt_camera* c, const mcrt_rend
     if (p->schedule != MCRT_SCHEDULE_STREAM && p->schedule != MCRT_SCHEDULE_WAVES)
         return fail(MCRT_ERR_INVALID_ARGUMENT, "unknown schedule");
     if (p->reserved != 0) return fail(MCRT_ERR_INVALID_ARGUMENT, "reserved field must be 0");
+    if (p->path_chunk < 0 || p->path_chunk > kMaxQueue)
+        return fail(MCRT_ERR_INVALID_ARGUMENT, "path_chunk must be in [0, 2^27]");
     return MCRT_OK;
 }
 
@@ -1020,18 +986,17 @@ struct WaveEnqueue
     }
 };
 
-struct StreamEnqueue
+struct IterEnqueue
 {
     const WaveArgs*    a;
-    const StreamArgs*  x;
-    int                par;
+    int                p;
     const LaunchShape* ls;
     cudaStream_t       st;
     StageTimer*        tm;
     template <int S, bool C, int M>
     void run() const
     {
-        enqueue_stream_iter<S, C, M>(*a, *x, par, *ls, st, tm);
+        enqueue_iter<S, C, M>(*a, p, *ls, st, tm);
     }
 };
 
@@ -1055,19 +1020,28 @@ void with_variant(bool stack32, bool regcap, bool count, const F& f)
     }
 }
 
-int begin_run(Workspace& w, const std::vector<JobGPU>& jobs, cudaStream_t st, RunResult& run)
+// workspace, job table, zeroed statistics, pixel counts and counters; timing events
+int begin_run(Workspace& w, const std::vector<JobGPU>& jobs, int64_t capacity, int64_t ring, int64_t num_chunks,
+              cudaStream_t st, RunResult& run, WaveArgs& a)
 {
-    w.args.num_jobs = static_cast<int>(jobs.size());
+    int rc = ensure_workspace(w, capacity, ring, static_cast<int>(jobs.size()), num_chunks);
+    if (rc) return rc;
+    a = w.args;  // sub-arrays sized for at least `capacity` / `ring`; use exactly those
+    a.num_jobs = static_cast<int>(jobs.size());
+    a.capacity = capacity;
+    a.shadow_cap = 2 * capacity;
+    a.ring_size = ring;
     CK(cudaMemcpyAsync(w.jobs, jobs.data(), sizeof(JobGPU) * jobs.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(a.ring_cnt, 0, sizeof(int) * ring, st));
     CK(cudaEventCreate(&run.e0));
     CK(cudaEventCreate(&run.e1));
     return MCRT_OK;
 }
 
-// WAVES: path_chunk paths per wave (wave boundaries on pixel boundaries so a pixel's
-// samples resolve together), each wave runs to completion
+// WAVES: waves of at most path_chunk paths, on pixel boundaries; each wave is admitted
+// whole and runs until its last path is finished before the next is admitted
 int run_waves(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<int64_t>& pix_spp, int64_t total,
               int max_depth, int64_t path_chunk, bool stack32, bool regcap, bool count, bool stages, bool graph,
               const LaunchShape& lsv, cudaStream_t st, StageTimer& timer, RunResult& run)
@@ -1105,21 +1079,23 @@ int run_waves(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<i
     const int64_t num_chunks = static_cast<int64_t>(table.size()) - 1;
     int64_t       max_chunk = 0;
     for (int64_t k = 0; k < num_chunks; ++k) max_chunk = std::max(max_chunk, table[k + 1] - table[k]);
-    int rc = ensure_workspace(w, max_chunk, num_jobs, num_chunks);
-    if (rc) return rc;
-    rc = begin_run(w, jobs, st, run);
+    if (max_chunk > kMaxQueue) return fail(MCRT_ERR_INVALID_ARGUMENT, "one pixel's samples exceed the queue limit");
+    WaveArgs a;
+    // a wave's paths are all finished before the next wave is admitted: a ring of one
+    // wave never wraps onto a live entry
+    int rc = begin_run(w, jobs, max_chunk, max_chunk, num_chunks, st, run, a);
     if (rc) return rc;
     CK(cudaMemcpyAsync(w.chunk_table, table.data(), sizeof(int64_t) * table.size(), cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(w.ctrl, 0, sizeof(Ctrl), st));
     run.table_bytes = 8 * static_cast<int64_t>(table.size());
+    const int iters = wave_iterations(max_depth);
     run.waves = num_chunks;
-    run.launches = num_chunks * (3 + 3 * (max_depth + 1));
-    run.extend_launches = num_chunks * (max_depth + 1);
-    const WaveArgs a = w.args;
+    run.launches = 1 + num_chunks * (1 + 5 * iters);
+    run.extend_launches = num_chunks * iters;
     auto enqueue = [&](cudaStream_t s2, StageTimer* tm) {
         with_variant(stack32, regcap, count, WaveEnqueue{&a, max_depth, &lsv, s2, tm});
     };
     CK(cudaEventRecord(run.e0, st));
+    k_render_begin<<<1, 1, 0, st>>>(a, 1, 0);
     if (graph)
     {
         cudaGraph_t     g;
@@ -1146,80 +1122,32 @@ int run_waves(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<i
     return MCRT_OK;
 }
 
-size_t align256(size_t n) { return (n + 255) & ~static_cast<size_t>(255); }
-
-int ensure_stream(Workspace& w, int64_t slots, int64_t ring)
-{
-    if (w.s_capacity < slots)
-    {
-        cudaFree(w.s_block);
-        w.s_block = nullptr;
-        w.s_capacity = 0;
-        CK(cudaMalloc(&w.s_block, 2 * align256(4 * slots) + align256(8 * slots)));
-        w.s_capacity = slots;
-    }
-    if (w.s_ring < ring)
-    {
-        cudaFree(w.s_ring_block);
-        w.s_ring_block = nullptr;
-        w.s_ring = 0;
-        CK(cudaMalloc(&w.s_ring_block, align256(16 * ring) + align256(4 * ring)));
-        w.s_ring = ring;
-    }
-    if (!w.s_ctrl)
-    {
-        CK(cudaMalloc(&w.s_ctrl, sizeof(StreamCtrl)));
-        CK(cudaMallocHost(&w.h_poll, 2 * sizeof(unsigned long long)));
-    }
-    char* b = static_cast<char*>(w.s_block);
-    w.sargs.ctrl = w.s_ctrl;
-    w.sargs.dead[0] = reinterpret_cast<int*>(b);
-    w.sargs.dead[1] = reinterpret_cast<int*>(b + align256(4 * w.s_capacity));
-    w.sargs.gid = reinterpret_cast<int64_t*>(b + 2 * align256(4 * w.s_capacity));
-    char* r = static_cast<char*>(w.s_ring_block);
-    w.sargs.ring = reinterpret_cast<float4*>(r);
-    w.sargs.ring_cnt = reinterpret_cast<int*>(r + align256(16 * w.s_ring));
-    return MCRT_OK;
-}
-
-// STREAM: path_chunk slots refilled with new camera paths as paths end (see k_regen);
-// iterations run in graph-launched pairs (parity 0, 1) until every path is in the ring,
-// which the host learns from a device counter polled one batch behind the launches
+// STREAM: the queue is topped up with new camera paths every iteration; iterations run
+// in graph-launched pairs (parity 0, 1) until every path is finished, which the host
+// learns from a device counter polled one batch behind the launches
 int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<int64_t>& pix_spp, int64_t total,
                int max_depth, int64_t path_chunk, bool stack32, bool regcap, bool count, bool stages, bool graph,
                const LaunchShape& lsv, cudaStream_t st, StageTimer& timer, RunResult& run)
 {
-    const int num_jobs = static_cast<int>(jobs.size());
-    int64_t   slots = path_chunk > 0 ? path_chunk : (int64_t(1) << 21);
-    slots = std::min(slots, (total + 31) / 32 * 32);
-    slots = std::max<int64_t>(slots, 64);
-    if (slots > (int64_t(1) << 30)) return fail(MCRT_ERR_INVALID_ARGUMENT, "path_chunk too large");
+    int64_t capacity = path_chunk > 0 ? path_chunk : kDefaultQueue;
+    capacity = std::min(capacity, (total + 31) / 32 * 32);
+    capacity = std::max<int64_t>(capacity, 64);
     int64_t max_spp = 1;
     for (int64_t v : pix_spp) max_spp = std::max(max_spp, v);
-    const int64_t ring = std::min(total, (max_depth + 2) * slots + max_spp);
-    int           rc = ensure_workspace(w, slots, num_jobs, 0);
+    const int64_t ring = stream_ring_entries(capacity, max_depth, max_spp, total);
+    WaveArgs      a;
+    int           rc = begin_run(w, jobs, capacity, ring, 0, st, run, a);
     if (rc) return rc;
-    rc = ensure_stream(w, slots, ring);
-    if (rc) return rc;
-    rc = begin_run(w, jobs, st, run);
-    if (rc) return rc;
-    WaveArgs a = w.args;  // sub-arrays sized for >= slots; use exactly `slots`
-    a.capacity = slots;
-    a.shadow_cap = 2 * slots;
-    StreamArgs x = w.sargs;
-    x.ring_size = ring;
-    x.total = total;
-    CK(cudaMemsetAsync(x.ctrl, 0, sizeof(StreamCtrl), st));
-    CK(cudaMemsetAsync(x.ring_cnt, 0, sizeof(int) * ring, st));
-    auto iter = [&](cudaStream_t s2, int par, StageTimer* tm) {
-        with_variant(stack32, regcap, count, StreamEnqueue{&a, &x, par, &lsv, s2, tm});
+    auto iter = [&](cudaStream_t s2, int p, StageTimer* tm) {
+        with_variant(stack32, regcap, count, IterEnqueue{&a, p, &lsv, s2, tm});
     };
-    // a slot holds one path for at most max_depth + 1 iterations and starts the next in
-    // the iteration that ends it: every path is in the ring after this many iterations
-    const int64_t bound = ((total + slots - 1) / slots + 1) * (max_depth + 1) + 2;
+    // while paths remain to be admitted every iteration traces a full queue, each path
+    // has at most max_depth + 1 rays in queues, and a path is finished at most
+    // max_depth + 2 iterations after admission
+    const int64_t bound = (total * (max_depth + 1) + capacity - 1) / capacity + max_depth + 2;
     constexpr int kPairsPerPoll = 4;
     CK(cudaEventRecord(run.e0, st));
-    k_stream_init<<<lsv.grid_small, 256, 0, st>>>(a, x);
+    k_render_begin<<<1, 1, 0, st>>>(a, 0, total);
     run.launches = 1;
     cudaGraph_t     g = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1243,12 +1171,11 @@ int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<
             return fail(MCRT_ERR_CUDA, std::string("stream graph: ") + cudaGetErrorString(e));
         }
     }
-    cudaEvent_t poll_ev[2];
-    CK(cudaEventCreateWithFlags(&poll_ev[0], cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&poll_ev[1], cudaEventDisableTiming));
-    int64_t     iters = 0;
-    cudaError_t e = cudaSuccess;
-    bool        done = false;
+    cudaEvent_t poll_ev[2] = {nullptr, nullptr};
+    cudaError_t e = cudaEventCreateWithFlags(&poll_ev[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&poll_ev[1], cudaEventDisableTiming);
+    int64_t iters = 0;
+    bool    done = false;
     for (int b = 0; !done && e == cudaSuccess; ++b)
     {
         for (int k = 0; k < kPairsPerPoll && e == cudaSuccess; ++k)
@@ -1266,7 +1193,7 @@ int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<
             iters += 2;
         }
         if (e != cudaSuccess) break;
-        e = cudaMemcpyAsync(&w.h_poll[b & 1], &x.ctrl->finished, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+        e = cudaMemcpyAsync(&w.h_poll[b & 1], &a.ctrl->finished, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                             st);
         if (e == cudaSuccess) e = cudaEventRecord(poll_ev[b & 1], st);
         run.poll_bytes += sizeof(unsigned long long);
@@ -1275,7 +1202,7 @@ int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<
             e = cudaEventSynchronize(poll_ev[(b - 1) & 1]);
             if (e == cudaSuccess && static_cast<int64_t>(w.h_poll[(b - 1) & 1]) >= total) done = true;
         }
-        if (!done && iters > bound + 4 * kPairsPerPoll)
+        if (e == cudaSuccess && !done && iters > bound + 4 * kPairsPerPoll)
         {
             cudaStreamSynchronize(st);
             cudaEventDestroy(poll_ev[0]);
@@ -1286,8 +1213,8 @@ int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<
     }
     if (e == cudaSuccess) e = cudaEventRecord(run.e1, st);
     if (e == cudaSuccess && graph) e = cudaStreamSynchronize(st);  // before the graph is destroyed
-    cudaEventDestroy(poll_ev[0]);
-    cudaEventDestroy(poll_ev[1]);
+    if (poll_ev[0]) cudaEventDestroy(poll_ev[0]);
+    if (poll_ev[1]) cudaEventDestroy(poll_ev[1]);
     release_graph();
     if (e != cudaSuccess) return fail(MCRT_ERR_CUDA, std::string("streaming render: ") + cudaGetErrorString(e));
     run.waves = iters;
@@ -1433,49 +1360,76 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
 
 namespace mcrt {
 
-size_t wave_bytes(int64_t capacity)
+namespace {
+// sub-array allocator: 256-B aligned pieces of one block
+struct Carver
 {
-    const int64_t C = capacity, S = 2 * capacity;
-    // per path: qo, qd x2 (64 B), qp x2 (8), hits 16, thr 16, rad 16, rng 8, pix 4, job 4,
-    // nee_val 64, pend 4; next-event queues: 2 x S x (so, sd, sv 48 B + sm 16 B);
-    // plus 256-B alignment of each of the 22 sub-arrays
-    return static_cast<size_t>(C) * (64 + 8 + 16 + 16 + 16 + 8 + 4 + 4 + 64 + 4) + static_cast<size_t>(S) * 2 * 64 +
-           256 * 24;
-}
-
-void carve_wave(WaveArgs& a, void* base, int64_t capacity)
-{
-    const int64_t C = capacity, S = 2 * capacity;
-    char*         p = static_cast<char*>(base);
-    auto          take = [&](size_t n) {
+    char* p;
+    void* take(size_t n)
+    {
         size_t off = (reinterpret_cast<uintptr_t>(p) + 255) & ~static_cast<uintptr_t>(255);
         char*  r = reinterpret_cast<char*>(off);
         p = r + n;
-        return static_cast<void*>(r);
-    };
-    for (int k = 0; k < 2; ++k)
-    {
-        a.qo[k] = static_cast<float4*>(take(16 * C));
-        a.qd[k] = static_cast<float4*>(take(16 * C));
-        a.qp[k] = static_cast<int*>(take(4 * C));
+        return r;
     }
-    a.hits = static_cast<float4*>(take(16 * C));
-    a.thr = static_cast<float4*>(take(16 * C));
-    a.rad = static_cast<float4*>(take(16 * C));
-    a.rng = static_cast<uint64_t*>(take(8 * C));
-    a.pix = static_cast<int*>(take(4 * C));
-    a.job = static_cast<int*>(take(4 * C));
-    a.nee_val = static_cast<float4*>(take(64 * C));
-    a.pend = static_cast<int*>(take(4 * C));
+};
+}  // namespace
+
+size_t queue_bytes(int64_t capacity)
+{
+    const size_t C = static_cast<size_t>(capacity);
+    // by parity: qo, qd, qthr, qrad (64 B) + qrng 8 + drad, dmeta 32 + nev 128; hits 16;
+    // next-event queues: 2 x 2C x (so, sd, sv, sm) 64 B; 256-B alignment of 31 sub-arrays
+    return 2 * C * (64 + 8 + 32 + 128) + C * 16 + 2 * (2 * C) * 64 + 256 * 32;
+}
+
+void carve_queues(WaveArgs& a, void* base, int64_t capacity)
+{
+    const int64_t C = capacity, S = 2 * capacity;
+    Carver        c{static_cast<char*>(base)};
     for (int k = 0; k < 2; ++k)
     {
-        a.so[k] = static_cast<float4*>(take(16 * S));
-        a.sd[k] = static_cast<float4*>(take(16 * S));
-        a.sv[k] = static_cast<float4*>(take(16 * S));
-        a.sm[k] = static_cast<int4*>(take(16 * S));
+        a.qo[k] = static_cast<float4*>(c.take(16 * C));
+        a.qd[k] = static_cast<float4*>(c.take(16 * C));
+        a.qthr[k] = static_cast<float4*>(c.take(16 * C));
+        a.qrad[k] = static_cast<float4*>(c.take(16 * C));
+        a.qrng[k] = static_cast<uint64_t*>(c.take(8 * C));
+        a.drad[k] = static_cast<float4*>(c.take(16 * C));
+        a.dmeta[k] = static_cast<int4*>(c.take(16 * C));
+        a.nev[k] = static_cast<float4*>(c.take(128 * C));
+    }
+    a.hits = static_cast<float4*>(c.take(16 * C));
+    for (int k = 0; k < 2; ++k)
+    {
+        a.so[k] = static_cast<float4*>(c.take(16 * S));
+        a.sd[k] = static_cast<float4*>(c.take(16 * S));
+        a.sv[k] = static_cast<float4*>(c.take(16 * S));
+        a.sm[k] = static_cast<int4*>(c.take(16 * S));
     }
     a.capacity = C;
     a.shadow_cap = S;
+}
+
+size_t ring_bytes(int64_t entries) { return 16 * static_cast<size_t>(entries) + 4 * static_cast<size_t>(entries) + 512; }
+
+void carve_ring(WaveArgs& a, void* base, int64_t entries)
+{
+    Carver c{static_cast<char*>(base)};
+    a.ring = static_cast<float4*>(c.take(16 * entries));
+    a.ring_cnt = static_cast<int*>(c.take(4 * entries));
+    a.ring_size = entries;
+}
+
+int64_t stream_ring_entries(int64_t capacity, int max_depth, int64_t max_spp, int64_t total)
+{
+    return std::min(total, (max_depth + 2) * capacity + max_spp);
+}
+
+int wave_iterations(int max_depth) { return (max_depth + 2 + 1) & ~1; }
+
+void enqueue_render_begin(const WaveArgs& a, bool waves, int64_t limit, cudaStream_t st)
+{
+    k_render_begin<<<1, 1, 0, st>>>(a, waves ? 1 : 0, limit);
 }
 
 LaunchShape launch_shape() { return launch_shape_variant(false, false); }
@@ -1854,7 +1808,7 @@ static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_came
         dge = static_cast<float*>(a3);
     }
     Workspace& w = owner->ws;
-    int        rc = ensure_workspace(w, 64, num_jobs, 1);
+    int        rc = ensure_workspace(w, 0, 0, num_jobs, 1);
     if (rc)
     {
         cleanup();

@@ -3,12 +3,13 @@
 // (cudaMalloc is not capturable), plug-ins that live inside a host application's own
 // device-memory pool or arena, or callers that run under a hard memory budget.
 //
-// The wavefront needs scratch memory for its queues and path state.  Here it lives in a
-// file-scope static __device__ array of fixed size (kNoAllocScratchBytes): no
-// cudaMalloc, cudaFree, event, graph or library allocation happens in the call.  The
-// array belongs to this file's module, so every GPU that loads it holds it until the
-// process exits.  Waves are limited to kNoAllocPaths path slots and a render to
-// kNoAllocWaves waves; requests beyond either are rejected with MCRT_ERR_INVALID_ARGUMENT.
+// The wavefront needs scratch memory for its queues, its per-path ring and its counters.
+// Here it lives in a file-scope static __device__ array of fixed size
+// (kNoAllocScratchBytes): no cudaMalloc, cudaFree, event, graph or library allocation
+// happens in the call.  The array belongs to this file's module, so every GPU that loads
+// it holds it until the process exits.  The render runs the wave schedule with waves of
+// at most kNoAllocPaths paths and at most kNoAllocWaves waves; requests beyond either are
+// rejected with MCRT_ERR_INVALID_ARGUMENT.
 //
 // Host code cannot use the array's name as a device address (on the host it is a
 // stand-in).  The first call on a device takes the array's device address with
@@ -27,13 +28,14 @@
 namespace mcrt {
 namespace {
 
-constexpr int64_t kNoAllocPaths = 65536;  // path slots per wave
+constexpr int64_t kNoAllocPaths = 65536;  // paths per wave (rays per queue)
 constexpr int64_t kNoAllocWaves = 65536;  // waves per render
 constexpr size_t  kHeaderBytes = 4096;    // Ctrl, stats, error word, one JobGPU
 constexpr size_t  kChunkBytes = sizeof(int64_t) * (kNoAllocWaves + 1);
-// wave_bytes(kNoAllocPaths), rounded up; checked against wave_bytes() at set-up
-constexpr size_t kWaveBytes = (static_cast<size_t>(kNoAllocPaths) * 460 + 256 * 32 + 255) & ~size_t(255);
-constexpr size_t kNoAllocScratchBytes = kHeaderBytes + kChunkBytes + kWaveBytes;
+// queue_bytes(kNoAllocPaths) and ring_bytes(kNoAllocPaths), rounded up; checked at set-up
+constexpr size_t kQueueBytes = (static_cast<size_t>(kNoAllocPaths) * 736 + 256 * 32 + 255) & ~size_t(255);
+constexpr size_t kRingBytes = (static_cast<size_t>(kNoAllocPaths) * 20 + 512 + 255) & ~size_t(255);
+constexpr size_t kNoAllocScratchBytes = kHeaderBytes + kChunkBytes + kQueueBytes + kRingBytes;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -48,7 +50,8 @@ struct Layout
     int*                err;
     JobGPU*             job;
     int64_t*            chunks;
-    void*               wave;
+    void*               queues;
+    void*               ring;
 };
 
 Layout layout(void* base)
@@ -60,7 +63,8 @@ Layout layout(void* base)
     l.err = reinterpret_cast<int*>(p + 2048 + 8 * sizeof(unsigned long long));
     l.job = reinterpret_cast<JobGPU*>(p + 2304);
     l.chunks = reinterpret_cast<int64_t*>(p + kHeaderBytes);
-    l.wave = p + kHeaderBytes + kChunkBytes;
+    l.queues = p + kHeaderBytes + kChunkBytes;
+    l.ring = p + kHeaderBytes + kChunkBytes + kQueueBytes;
     return l;
 }
 static_assert(sizeof(Ctrl) <= 2048, "Ctrl must fit the scratch header");
@@ -118,7 +122,7 @@ extern "C" int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera,
             std::lock_guard<std::mutex> lock(g_setup_mu);
             if (!g_scratch_ptr[dev])
             {
-                if (wave_bytes(kNoAllocPaths) > kWaveBytes)
+                if (queue_bytes(kNoAllocPaths) > kQueueBytes || ring_bytes(kNoAllocPaths) > kRingBytes)
                     return set_error(MCRT_ERR_INTERNAL, "no-alloc scratch smaller than one wave's state");
                 void* p = nullptr;
                 e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -144,7 +148,8 @@ extern "C" int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera,
         J.path_offset = 0;
         J.image = rgb_out_device;
         WaveArgs a{};
-        carve_wave(a, L.wave, kNoAllocPaths);
+        carve_queues(a, L.queues, kNoAllocPaths);
+        carve_ring(a, L.ring, kNoAllocPaths);  // a wave's paths finish before the next wave starts
         a.ctrl = L.ctrl;
         a.chunk_table = L.chunks;
         a.jobs = L.job;
@@ -152,13 +157,14 @@ extern "C" int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera,
         a.stats = L.stats;
         a.err = L.err;
         // the array keeps the previous call's contents: clear what must start at zero
-        e = cudaMemsetAsync(L.ctrl, 0, sizeof(Ctrl), st);
-        if (e == cudaSuccess) e = cudaMemsetAsync(L.stats, 0, 8 * sizeof(unsigned long long), st);
+        e = cudaMemsetAsync(L.stats, 0, 8 * sizeof(unsigned long long), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(L.err, 0, sizeof(int), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(a.ring_cnt, 0, sizeof(int) * kNoAllocPaths, st);
         if (e != cudaSuccess) return set_error(MCRT_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
         k_noalloc_setup<<<static_cast<int>((waves + 256) / 256), 256, 0, st>>>(J, L.job, L.chunks, total, per_wave,
                                                                              waves);
         LaunchShape ls = launch_shape();
+        enqueue_render_begin(a, true, 0, st);
         for (int64_t k = 0; k < waves; ++k) enqueue_wave_plain(a, params->max_depth, ls, st);
         e = cudaGetLastError();
         if (e != cudaSuccess) return set_error(MCRT_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
@@ -175,8 +181,9 @@ extern "C" int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera,
             stats->extension_rays = static_cast<int64_t>(hstats[0]);
             stats->shadow_rays = static_cast<int64_t>(hstats[1]);
             stats->waves = static_cast<int32_t>(waves);
-            stats->kernel_launches = static_cast<int32_t>(1 + waves * (3 + 3 * (params->max_depth + 1)));
-            stats->extend_launches = static_cast<int32_t>(waves * (params->max_depth + 1));
+            const int iters = wave_iterations(params->max_depth);
+            stats->kernel_launches = static_cast<int32_t>(2 + waves * (1 + 5 * iters));
+            stats->extend_launches = static_cast<int32_t>(waves * iters);
             stats->d2h_bytes = static_cast<int64_t>(sizeof(hstats) + sizeof(herr));
         }
         if (herr & 1) return set_error(MCRT_ERR_STACK_OVERFLOW, "traversal stack overflow");

@@ -1,6 +1,22 @@
-// Wavefront state shared by the render entry points (kernels.cu, noalloc.cu): the per-
-// wave control block, the SoA path-state layout, and the host helpers that lay it out
-// and enqueue one wave of stage kernels.
+// Wavefront state shared by the render entry points (kernels.cu, noalloc.cu): the control
+// block, the SoA layout of the queues, and the host helpers that lay it out and enqueue
+// iterations of stage kernels.
+//
+// Path state travels with its ray through the queues (no per-path slots): every stage
+// reads and writes its items by queue position, so all per-path traffic is coalesced.
+// One iteration (parity p = iteration & 1):
+//   k_iter_begin  zero the counters this iteration appends to; admit new paths: the
+//                 queue is topped up to its capacity from the path counter, bounded by
+//                 the admission limit (the whole render when streaming, the current wave
+//                 for the wave schedule)
+//   k_regen       finish the paths that ended in the previous iteration (their
+//                 next-event results are in): radiance into the ring, pixel resolved in
+//                 sample order when its last path finished; start the admitted paths
+//   k_extend      closest hit of every ray of queue p
+//   k_shade       one vertex per ray: continuing paths to queue p ^ 1, ended paths to
+//                 the finished list p ^ 1, next-event rays to the next-event queues
+//   k_connect     trace the next-event rays; each result goes to the slot its path
+//                 will read next (queue p ^ 1 position or finished-list position)
 #pragma once
 #include <cuda_runtime.h>
 
@@ -15,78 +31,61 @@ namespace mcrt {
 constexpr int kTraceBlock = 128;
 constexpr int kStack = 64;
 constexpr int kMaxDepth = 62;
+constexpr int64_t kMaxQueue = int64_t(1) << 27;     // rays per queue (result indices stay in int)
+constexpr int64_t kDefaultQueue = int64_t(1) << 21;  // streaming schedule default
 
-// per-wave control block: the wave's path range and the queue counters of every depth
+// counters of one render
 struct Ctrl
 {
-    int64_t base;
-    int     count;
-    int     chunk;
-    int     qcount[kMaxDepth + 2];
-    int     scount[kMaxDepth + 1][2];
+    int                qcount[2];  // ray queues (by parity)
+    int                dcount[2];  // lists of finished paths (by parity)
+    int                scount[2];  // next-event queues of the current iteration: any-hit, closest-hit
+    int                new_base;   // this iteration's admitted paths: first queue position
+    int                new_count;  //   and how many
+    int                chunk;      // wave schedule: index of the current wave
+    int                pad;
+    unsigned long long next;      // index of the next path to admit
+    unsigned long long limit;     // admission limit (exclusive)
+    unsigned long long new_g;     // index of the first path admitted this iteration
+    unsigned long long finished;  // paths whose radiance reached the ring
 };
 
-// device pointers of one wave's state (SoA, `capacity` path slots)
+// device pointers of one render's state (SoA, `capacity` rays per queue)
 struct WaveArgs
 {
-    Ctrl*               ctrl;
-    const int64_t*      chunk_table;
-    const JobGPU*       jobs;
-    int                 num_jobs;
-    int64_t             capacity;
-    float4*             qo[2];  // ray queues (ping-pong by depth): origin + tmin
-    float4*             qd[2];  //   direction + tmax
-    int*                qp[2];  //   path slot of each queued ray
-    float4*             hits;
-    float4*             thr;      // throughput + flags
-    float4*             rad;      // radiance gathered so far
-    uint64_t*           rng;      // PCG32 state
-    int*                pix;
-    int*                job;
-    float4*             nee_val;  // 4 next-event results per path slot (written by k_connect)
-    int*                pend;     // per path slot: mask of next-event results not yet added
-    float4*             so[2];    // next-event queues: [0] any-hit, [1] closest-hit
-    float4*             sd[2];
-    float4*             sv[2];
-    int4*               sm[2];
-    int64_t             shadow_cap;
+    Ctrl*          ctrl;
+    const int64_t* chunk_table;  // wave schedule: wave boundaries (path indices)
+    const JobGPU*  jobs;
+    int            num_jobs;
+    int64_t        capacity;
+    // ray queues by parity.  o.w = job index, d.w = pixel index (int bits; extension rays
+    // always span [kEpsRay, inf)); thr.w = flags | vertex << 8 | pending mask << 16;
+    // rad.w = sample index (int bits)
+    float4*   qo[2];
+    float4*   qd[2];
+    float4*   qthr[2];
+    float4*   qrad[2];
+    uint64_t* qrng[2];
+    float4*   hits;  // by position of the current queue
+    // finished paths by parity: radiance (w = sample), {pixel, job, pending mask, 0}
+    float4* drad[2];
+    int4*   dmeta[2];
+    // next-event results by parity: [4 i + s] for queue position i, [4 capacity + 4 j + s]
+    // for finished-list position j
+    float4* nev[2];
+    // next-event queues: [0] any-hit, [1] closest-hit; meta = {result index, type, light, job}
+    float4* so[2];
+    float4* sd[2];
+    float4* sv[2];
+    int4*   sm[2];
+    int64_t shadow_cap;
+    // per-path radiance of path g at g % ring_size until its pixel resolves; per pixel
+    // (at its first path's ring index) the count of its finished paths
+    float4*             ring;
+    int*                ring_cnt;
+    int64_t             ring_size;
     unsigned long long* stats;  // [0] extension rays, [1] next-event rays, [2..5] work counters
     int*                err;
-};
-
-// queues one k_shade launch reads and appends to (counts live in device memory)
-struct QueueSel
-{
-    const int* count;       // rays in the input queue
-    int        qs;          // input ray queue; continuing rays go to queue qs ^ 1
-    int*       next_count;  // append counter of queue qs ^ 1
-    int*       scount;      // [2] append counters of the next-event queues (any-hit, closest-hit)
-    int*       dead_count;  // streaming: append counter of the list of slots whose path ended
-    int*       dead;        //   and the list (nullptr for waves)
-    int        depth;       // waves: the vertex index of every queued path; streaming: -1
-                            // (each slot keeps its own in bits 8.. of thr.w)
-};
-
-// streaming schedule: counters of one render (iteration parity selects the queue pair)
-struct StreamCtrl
-{
-    int                qcount[2];  // ray queues
-    int                dcount[2];  // lists of slots whose path ended
-    int                scount[2];  // next-event queues of the current iteration
-    int                pad[2];
-    unsigned long long next;       // index of the next path to start
-    unsigned long long finished;   // paths whose radiance is in the ring
-};
-
-struct StreamArgs
-{
-    StreamCtrl* ctrl;
-    int*        dead[2];    // slot lists by iteration parity
-    int64_t*    gid;        // path index held by each slot, -1: none
-    float4*     ring;       // radiance of path g at g % ring_size (until its pixel resolves)
-    int*        ring_cnt;   // per pixel, at its first path's ring index: paths finished
-    int64_t     ring_size;
-    int64_t     total;      // paths of the render
 };
 
 struct LaunchShape
@@ -94,14 +93,27 @@ struct LaunchShape
     int grid_trace, grid_shade, grid_small, block;
 };
 
-// bytes of the per-path arrays for `capacity` slots (256-B aligned sub-arrays)
-size_t wave_bytes(int64_t capacity);
-// lays the per-path arrays out in [base, base + wave_bytes(capacity))
-void carve_wave(WaveArgs& a, void* base, int64_t capacity);
+// bytes of the queues for `capacity` rays (256-B aligned sub-arrays)
+size_t queue_bytes(int64_t capacity);
+// lays the queues out in [base, base + queue_bytes(capacity))
+void carve_queues(WaveArgs& a, void* base, int64_t capacity);
+// bytes of a ring of `entries` paths (radiance + per-pixel counts)
+size_t ring_bytes(int64_t entries);
+void   carve_ring(WaveArgs& a, void* base, int64_t entries);
+// ring entries the streaming schedule needs: paths admitted during the lifetime of one
+// path (a path is finished at most max_depth + 2 iterations after admission, at most
+// `capacity` paths are admitted per iteration) plus one pixel's samples
+int64_t stream_ring_entries(int64_t capacity, int max_depth, int64_t max_spp, int64_t total);
+// iterations of one wave of the wave schedule (even, so every wave starts on parity 0)
+int wave_iterations(int max_depth);
 // persistent grid sizes from the SM count and occupancy (queries only, no allocation)
 LaunchShape launch_shape();
 LaunchShape launch_shape_variant(bool stack32, bool regcap);
-// one wave of stage launches on `st`: begin, raygen, (extend, shade, connect) x depth, resolve
+// starts a render: zeroes the counters and sets the admission limit (`limit`; with `waves`
+// nothing is admitted until the first wave's k_wave_next) -- one kernel, so it may run
+// inside a stream capture; the per-pixel counts of the ring must be zero
+void enqueue_render_begin(const WaveArgs& a, bool waves, int64_t limit, cudaStream_t st);
+// one wave of the wave schedule with the plain kernels (no counters, 64-entry stacks)
 void enqueue_wave_plain(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st);
 // Camera::Camera in float with the reference's operation order
 CameraGPU make_camera(const mcrt_camera& c);
