@@ -175,6 +175,80 @@ __global__ void k_iter_begin(WaveArgs a, int p)
     c->next += static_cast<unsigned long long>(n);
 }
 
+// Gradient accumulators of an adjoint launch: per block in shared memory (flushed with
+// one global atomic per nonzero entry when the block ends) or straight to the global
+// vectors when they do not fit.
+struct Grads
+{
+    float* ga;
+    float* ge;
+};
+
+template <bool ADJ>
+__device__ __forceinline__ Grads grads_begin(const WaveArgs& a, float* sgrad)
+{
+    Grads g{a.g_albedo, a.g_emis};
+    if (ADJ && a.grad_shared)
+    {
+        const int ng = 3 * (a.n_albedo + a.n_emis);
+        for (int k = threadIdx.x; k < ng; k += blockDim.x) sgrad[k] = 0.f;
+        __syncthreads();
+        g.ga = sgrad;
+        g.ge = sgrad + 3 * a.n_albedo;
+    }
+    return g;
+}
+
+template <bool ADJ>
+__device__ __forceinline__ void grads_end(const WaveArgs& a, const float* sgrad)
+{
+    if (!ADJ || !a.grad_shared) return;
+    __syncthreads();
+    const int na = 3 * a.n_albedo, ng = 3 * (a.n_albedo + a.n_emis);
+    for (int k = threadIdx.x; k < ng; k += blockDim.x)
+    {
+        const float v = sgrad[k];
+        if (v != 0.f)
+        {
+            if (k < na)
+                atomicAdd(&a.g_albedo[k], v);
+            else
+                atomicAdd(&a.g_emis[k - na], v);
+        }
+    }
+}
+
+__device__ __forceinline__ void add_grad3(float* g, int idx, float3 v)
+{
+    atomicAdd(&g[3 * idx + 0], v.x);
+    atomicAdd(&g[3 * idx + 1], v.y);
+    atomicAdd(&g[3 * idx + 2], v.z);
+}
+
+// dL/d(sample radiance) of a path: dL/dimage at its pixel / spp
+__device__ __forceinline__ float3 path_dl(const JobGPU& J, int pixel)
+{
+    const float* g = J.image + 3 * static_cast<int64_t>(pixel);
+    return mk(g[0], g[1], g[2]) * (1.0f / J.spp);
+}
+
+// the k-th 16-bit material id of a path's adjoint log (two uint4 = 8 words)
+__device__ __forceinline__ int log_get(const unsigned* w, int k)
+{
+    unsigned v = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        if (q == (k >> 1)) v = w[q];
+    return static_cast<int>((v >> (16 * (k & 1))) & 0xffffu);
+}
+
+__device__ __forceinline__ void log_put(unsigned* w, int k, int matid)
+{
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        if (q == (k >> 1)) w[q] |= static_cast<unsigned>(matid & 0xffff) << (16 * (k & 1));
+}
+
 // starts camera path g (sample s of pixel x, y of its job) at position `pos` of ray
 // queue p (demo_pt.cpp:689-700)
 __device__ __forceinline__ void start_camera_path(const WaveArgs& a, int64_t g, int p, int pos)
@@ -208,8 +282,37 @@ __device__ __forceinline__ void start_camera_path(const WaveArgs& a, int64_t g, 
 // Finishes the warp's ended paths (lanes with `valid`): radiance into the ring; a pixel
 // whose last path this was is resolved by the whole warp from the ring in sample order,
 // with the arithmetic of FrameBuffer::accumulatePixel / scale.  Called by all 32 lanes.
-__device__ __forceinline__ void finish_paths(const WaveArgs& a, int p, int i, bool valid, unsigned long long& fin)
+//
+// Adjoint (ADJ): the path's radiance L is final here, so each logged Lambert vertex k
+// gets + dL/dI * L / albedo_k; k_shade already added - dL/dI * L_before(k) / albedo_k.
+// Together: (L - L_before(k)) / albedo_k, the path-replay albedo derivative.  A path
+// whose L is NaN is scrubbed by the forward (demo_pt.cpp:653) and gets no + term.
+template <bool ADJ>
+__device__ __forceinline__ void finish_paths(const WaveArgs& a, const Grads& G, int p, int i, bool valid,
+                                             unsigned long long& fin)
 {
+    if (ADJ)
+    {
+        if (!valid) return;
+        const int4    m = a.dmeta[p][i];
+        const float4 r = add_pending(a.nev[p] + 4 * a.capacity + 4 * static_cast<int64_t>(i), m.z, a.drad[p][i]);
+        ++fin;
+        if (isnan3(xyz(r)) || m.w == 0) return;
+        const JobGPU&    J = a.jobs[m.y];
+        const SceneView& S = J.scene;
+        const float3     dl = path_dl(J, m.x);
+        const uint4      l0 = a.dlog[p][2 * static_cast<int64_t>(i)], l1 = a.dlog[p][2 * static_cast<int64_t>(i) + 1];
+        const unsigned   w[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+        for (int k = 0; k < m.w; ++k)
+        {
+            const MaterialGPU& M = S.materials[log_get(w, k)];
+            const int          pk = M.albedo_param;
+            if (M.r > 0.f) atomicAdd(&G.ga[3 * pk + 0], dl.x * r.x / M.r);
+            if (M.g > 0.f) atomicAdd(&G.ga[3 * pk + 1], dl.y * r.y / M.g);
+            if (M.b > 0.f) atomicAdd(&G.ga[3 * pk + 2], dl.z * r.z / M.b);
+        }
+        return;
+    }
     const int     lane = threadIdx.x & 31;
     const int64_t R = a.ring_size;
     int64_t       cidx = 0;
@@ -286,8 +389,11 @@ __device__ __forceinline__ void finish_paths(const WaveArgs& a, int p, int i, bo
     }
 }
 
+template <bool ADJ>
 __global__ void __launch_bounds__(128) k_regen(WaveArgs a, int p)
 {
+    extern __shared__ float sgrad[];
+    const Grads        G = grads_begin<ADJ>(a, sgrad);
     const Ctrl*        c = a.ctrl;
     const int          nd = min(c->dcount[p], static_cast<int>(a.capacity));
     const int          nn = c->new_count;
@@ -300,11 +406,12 @@ __global__ void __launch_bounds__(128) k_regen(WaveArgs a, int p)
     for (int wbase = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < n; wbase += warps_total * 32)
     {
         const int i = wbase + lane;
-        if (wbase < nd) finish_paths(a, p, i, i < nd, fin);
+        if (wbase < nd) finish_paths<ADJ>(a, G, p, i, i < nd, fin);
         if (i < nn) start_camera_path(a, g0 + i, p, nb + i);
     }
     for (int off = 16; off > 0; off >>= 1) fin += __shfl_down_sync(0xffffffffu, fin, off);
     if (lane == 0 && fin) atomicAdd(&a.ctrl->finished, fin);
+    grads_end<ADJ>(a, sgrad);
 }
 
 template <int STACK, bool COUNT, int MINB>
@@ -328,8 +435,14 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
     if (COUNT) flush_count(a.stats, 2, cnt);
 }
 
+// Adjoint (ADJ): emission derivatives at emitter hits (the coefficient of E), and at a
+// parameterised Lambert vertex k the - dL/dI * L_before(k) / albedo_k half of the albedo
+// derivative; the vertex's material id goes to the path's log for the other half.
+template <bool ADJ>
 __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
 {
+    extern __shared__ float sgrad[];
+    const Grads G = grads_begin<ADJ>(a, sgrad);
     const int n = min(a.ctrl->qcount[p], static_cast<int>(a.capacity));
     const int lane = threadIdx.x & 31;
     const int warps_total = (gridDim.x * blockDim.x) >> 5;
@@ -341,9 +454,10 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
         bool     cont = false;
         float3   phit = mk(0.f, 0.f, 0.f), cdir = mk(0.f, 0.f, 1.f), T2 = mk(0.f, 0.f, 0.f);
         float4   rnew = make_float4(0.f, 0.f, 0.f, 0.f);
-        int      flags2 = 0, n_nee = 0, job = 0, pixel = 0;
+        int      flags2 = 0, n_nee = 0, job = 0, pixel = 0, nlog = 0;
         uint64_t rstate = 0;
         NeeRay   nee[4];
+        unsigned lw[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
         if (valid)
         {
             float4           o4 = a.qo[p][i], d4 = a.qd[p][i];
@@ -362,6 +476,19 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
             float3           Ladd = mk(0.f, 0.f, 0.f);
             // results of the previous vertex's next-event rays first, then this vertex
             float4 rp = add_pending(a.nev[p] + 4 * static_cast<int64_t>(i), (flags >> 16) & 0xf, a.qrad[p][i]);
+            float3 dl = mk(0.f, 0.f, 0.f);
+            if (ADJ)
+            {
+                dl = path_dl(J, pixel);
+                nlog = (flags >> 20) & 0x1f;
+                if (nlog > 0)
+                {
+                    const uint4 l0 = a.qlog[p][2 * static_cast<int64_t>(i)];
+                    const uint4 l1 = a.qlog[p][2 * static_cast<int64_t>(i) + 1];
+                    lw[0] = l0.x, lw[1] = l0.y, lw[2] = l0.z, lw[3] = l0.w;
+                    lw[4] = l1.x, lw[5] = l1.y, lw[6] = l1.z, lw[7] = l1.w;
+                }
+            }
             if (prim < 0)
             {
                 Ladd = miss_emission(S, d, T, no_direct);
@@ -374,10 +501,29 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
                 phit = o + d * hh.x;
                 if (m.type == MAT_LGHT)
                 {
-                    if (no_direct && dot3(d, ns) < 0.f) Ladd = T * m.color;
+                    if (no_direct && dot3(d, ns) < 0.f)
+                    {
+                        Ladd = T * m.color;
+                        if (ADJ && m.emission_param >= 0 && m.emission_param < a.n_emis)
+                            add_grad3(G.ge, m.emission_param, T * dl);
+                    }
                 }
                 else
                 {
+                    if (ADJ && m.type == MAT_DIFF && m.albedo_param >= 0 && m.albedo_param < a.n_albedo)
+                    {
+                        if (!isnan3(xyz(rp)))
+                        {
+                            const int pk = m.albedo_param;
+                            if (m.color.x > 0.f) atomicAdd(&G.ga[3 * pk + 0], -(dl.x * rp.x / m.color.x));
+                            if (m.color.y > 0.f) atomicAdd(&G.ga[3 * pk + 1], -(dl.y * rp.y / m.color.y));
+                            if (m.color.z > 0.f) atomicAdd(&G.ga[3 * pk + 2], -(dl.z * rp.z / m.color.z));
+                        }
+                        if (nlog < kAdjLog)
+                            log_put(lw, nlog++, matid);
+                        else
+                            atomicOr(a.err, kErrQueue);
+                    }
                     Pcg rng;
                     rng.state = a.qrng[p][i];
                     rng.inc = (static_cast<uint64_t>(pixel) << 1u) | 1u;
@@ -389,7 +535,7 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
                     bool   nee_here = does_nee(m.type);
                     if (nee_here) n_nee = make_nee(S, m, wi, ns, phit, T, u, nee);
                     cont = continue_path(m, wi, ns, T, u, depth, J.max_depth, J.rr_depth, T2, cdir);
-                    flags2 = (nee_here ? 1 : 0) | ((depth + 1) << 8);
+                    flags2 = (nee_here ? 1 : 0) | ((depth + 1) << 8) | (nlog << 20);
                 }
             }
             rnew = make_float4(rp.x + Ladd.x, rp.y + Ladd.y, rp.z + Ladd.z, rp.w);
@@ -414,6 +560,11 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
                     a.qthr[pn][k] = make_float4(T2.x, T2.y, T2.z, __int_as_float(flags2 | (pend << 16)));
                     a.qrad[pn][k] = rnew;
                     a.qrng[pn][k] = rstate;
+                    if (ADJ && nlog > 0)
+                    {
+                        a.qlog[pn][2 * static_cast<int64_t>(k)] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                        a.qlog[pn][2 * static_cast<int64_t>(k) + 1] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+                    }
                     dest = 4 * k;
                 }
                 else
@@ -434,7 +585,12 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
                 if (k < a.capacity)
                 {
                     a.drad[pn][k] = rnew;
-                    a.dmeta[pn][k] = make_int4(pixel, job, pend, 0);
+                    a.dmeta[pn][k] = make_int4(pixel, job, pend, ADJ ? nlog : 0);
+                    if (ADJ && nlog > 0)
+                    {
+                        a.dlog[pn][2 * static_cast<int64_t>(k)] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+                        a.dlog[pn][2 * static_cast<int64_t>(k) + 1] = make_uint4(lw[4], lw[5], lw[6], lw[7]);
+                    }
                     dest = static_cast<int>(4 * a.capacity) + 4 * k;
                 }
                 else
@@ -465,16 +621,21 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
                 a.so[qsel][idx] = make_float4(phit.x, phit.y, phit.z, kEpsRay);
                 a.sd[qsel][idx] = make_float4(nee[r].d.x, nee[r].d.y, nee[r].d.z, nee[r].tmax);
                 a.sv[qsel][idx] = nee[r].val;
-                a.sm[qsel][idx] = make_int4(dest + r, nee[r].type, nee[r].light, job);
+                a.sm[qsel][idx] = make_int4(dest + r, nee[r].type | (nee[r].light << 2), pixel, job);
             }
         }
     }
+    grads_end<ADJ>(a, sgrad);
 }
 
-template <int STACK, bool COUNT, int MINB>
+// Adjoint (ADJ): the emission derivative of each next-event contribution (the
+// coefficient of the reached emitter's E)
+template <int STACK, bool COUNT, int MINB, bool ADJ>
 __global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, int p)
 {
+    extern __shared__ float sgrad[];
     __shared__ int stack[STACK * kTraceBlock];
+    const Grads    G = grads_begin<ADJ>(a, sgrad);
     int*           st = stack + threadIdx.x;
     TraceCount     cnt = {0u, 0u};
     const int      n0 = min(a.ctrl->scount[0], static_cast<int>(a.shadow_cap));
@@ -496,10 +657,16 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, int p
                                                            h, a.err, &cnt);
         float3 coef;
         int    emat;
-        float3 add = nee_contribution(S, m.y, m.z, v, xyz(d), hit, h, coef, emat);
+        float3 add = nee_contribution(S, m.y & 3, m.y >> 2, v, xyz(d), hit, h, coef, emat);
         res[m.x] = make_float4(add.x, add.y, add.z, 0.f);
+        if (ADJ && emat >= 0)
+        {
+            const int ep = S.materials[emat].emission_param;
+            if (ep >= 0 && ep < a.n_emis) add_grad3(G.ge, ep, coef * path_dl(J, m.z));
+        }
     }
     if (COUNT) flush_count(a.stats, 4, cnt);
+    grads_end<ADJ>(a, sgrad);
 }
 
 // ---------------------------------------------------------------------------
@@ -721,8 +888,11 @@ struct Workspace
     unsigned long long* stats = nullptr;
     int*                err = nullptr;
     unsigned long long* h_poll = nullptr;  // pinned: completion polls of the streaming schedule
+    int64_t             adj_capacity = 0;    // rays per queue of `adj_block`
+    void*               adj_block = nullptr; // adjoint vertex logs
     void release()
     {
+        cudaFree(adj_block);
         cudaFree(block);
         cudaFree(ring_block);
         cudaFree(jobs);
@@ -907,8 +1077,8 @@ struct StageTimer
 
 // one iteration of parity p (five launches); stage timer slots: 0 begin + regen,
 // 1 extend, 2 shade, 3 connect
-template <int STACK, bool COUNT, int MINB>
-void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, StageTimer* tm)
+template <int STACK, bool COUNT, int MINB, bool ADJ = false>
+void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, StageTimer* tm, size_t dyn = 0)
 {
     auto beg = [&](int stg) {
         if (tm) tm->record(st, stg, true);
@@ -918,16 +1088,16 @@ void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t 
     };
     beg(0);
     k_iter_begin<<<1, 1, 0, st>>>(a, p);
-    k_regen<<<ls.grid_shade, 128, 0, st>>>(a, p);
+    k_regen<ADJ><<<ls.grid_shade, 128, dyn, st>>>(a, p);
     end();
     beg(1);
     k_extend<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, p);
     end();
     beg(2);
-    k_shade<<<ls.grid_shade, 128, 0, st>>>(a, p);
+    k_shade<ADJ><<<ls.grid_shade, 128, dyn, st>>>(a, p);
     end();
     beg(3);
-    k_connect<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, p);
+    k_connect<STACK, COUNT, MINB, ADJ><<<ls.grid_connect, kTraceBlock, dyn, st>>>(a, p);
     end();
 }
 
@@ -1034,7 +1204,7 @@ int begin_run(Workspace& w, const std::vector<JobGPU>& jobs, int64_t capacity, i
     CK(cudaMemcpyAsync(w.jobs, jobs.data(), sizeof(JobGPU) * jobs.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(w.stats, 0, sizeof(unsigned long long) * 8, st));
     CK(cudaMemsetAsync(w.err, 0, sizeof(int), st));
-    CK(cudaMemsetAsync(a.ring_cnt, 0, sizeof(int) * ring, st));
+    if (ring > 0) CK(cudaMemsetAsync(a.ring_cnt, 0, sizeof(int) * ring, st));
     CK(cudaEventCreate(&run.e0));
     CK(cudaEventCreate(&run.e1));
     return MCRT_OK;
@@ -1122,29 +1292,17 @@ int run_waves(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<i
     return MCRT_OK;
 }
 
-// STREAM: the queue is topped up with new camera paths every iteration; iterations run
-// in graph-launched pairs (parity 0, 1) until every path is finished, which the host
-// learns from a device counter polled one batch behind the launches
-int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<int64_t>& pix_spp, int64_t total,
-               int max_depth, int64_t path_chunk, bool stack32, bool regcap, bool count, bool stages, bool graph,
-               const LaunchShape& lsv, cudaStream_t st, StageTimer& timer, RunResult& run)
+// Iterations in graph-launched pairs (parity 0, 1) until every path is finished, which
+// the host learns from a device counter polled one batch behind the launches.
+// iter(stream, parity, timer) enqueues one iteration.
+template <class IterFn>
+int stream_loop(Workspace& w, const WaveArgs& a, int64_t total, int max_depth, bool stages, bool graph,
+                cudaStream_t st, StageTimer& timer, RunResult& run, const IterFn& iter)
 {
-    int64_t capacity = path_chunk > 0 ? path_chunk : kDefaultQueue;
-    capacity = std::min(capacity, (total + 31) / 32 * 32);
-    capacity = std::max<int64_t>(capacity, 64);
-    int64_t max_spp = 1;
-    for (int64_t v : pix_spp) max_spp = std::max(max_spp, v);
-    const int64_t ring = stream_ring_entries(capacity, max_depth, max_spp, total);
-    WaveArgs      a;
-    int           rc = begin_run(w, jobs, capacity, ring, 0, st, run, a);
-    if (rc) return rc;
-    auto iter = [&](cudaStream_t s2, int p, StageTimer* tm) {
-        with_variant(stack32, regcap, count, IterEnqueue{&a, p, &lsv, s2, tm});
-    };
     // while paths remain to be admitted every iteration traces a full queue, each path
     // has at most max_depth + 1 rays in queues, and a path is finished at most
     // max_depth + 2 iterations after admission
-    const int64_t bound = (total * (max_depth + 1) + capacity - 1) / capacity + max_depth + 2;
+    const int64_t bound = (total * (max_depth + 1) + a.capacity - 1) / a.capacity + max_depth + 2;
     constexpr int kPairsPerPoll = 4;
     CK(cudaEventRecord(run.e0, st));
     k_render_begin<<<1, 1, 0, st>>>(a, 0, total);
@@ -1221,6 +1379,99 @@ int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<
     run.launches += iters * 5;
     run.extend_launches = iters;
     return MCRT_OK;
+}
+
+// STREAM: the queue is topped up with new camera paths every iteration
+int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<int64_t>& pix_spp, int64_t total,
+               int max_depth, int64_t path_chunk, bool stack32, bool regcap, bool count, bool stages, bool graph,
+               const LaunchShape& lsv, cudaStream_t st, StageTimer& timer, RunResult& run)
+{
+    int64_t capacity = path_chunk > 0 ? path_chunk : kDefaultQueue;
+    capacity = std::min(capacity, (total + 31) / 32 * 32);
+    capacity = std::max<int64_t>(capacity, 64);
+    int64_t max_spp = 1;
+    for (int64_t v : pix_spp) max_spp = std::max(max_spp, v);
+    const int64_t ring = stream_ring_entries(capacity, max_depth, max_spp, total);
+    WaveArgs      a;
+    int           rc = begin_run(w, jobs, capacity, ring, 0, st, run, a);
+    if (rc) return rc;
+    auto iter = [&](cudaStream_t s2, int p, StageTimer* tm) {
+        with_variant(stack32, regcap, count, IterEnqueue{&a, p, &lsv, s2, tm});
+    };
+    return stream_loop(w, a, total, max_depth, stages, graph, st, timer, run, iter);
+}
+
+// Path-replay adjoint on the streaming wavefront: the forward's stages with ADJ set (see
+// k_shade, k_connect, finish_paths).  Needs max_depth < kAdjLog and material ids that fit
+// the 16-bit log.
+template <int STACK>
+void enqueue_adjoint_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, size_t dyn)
+{
+    enqueue_iter<STACK, false, 8, true>(a, p, ls, st, nullptr, dyn);
+}
+
+template <int STACK>
+int adjoint_launch_shape(size_t dyn, LaunchShape& ls)
+{
+    CK(cudaFuncSetAttribute(k_regen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
+    CK(cudaFuncSetAttribute(k_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
+    CK(cudaFuncSetAttribute(k_connect<STACK, false, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            static_cast<int>(dyn)));
+    const int sms = num_sms();
+    int       occ_e = 0, occ_s = 0, occ_c = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_extend<STACK, false, 8>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<true>, 128, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_connect<STACK, false, 8, true>, kTraceBlock, dyn);
+    ls.grid_trace = sms * std::max(occ_e, 1);
+    ls.grid_connect = sms * std::max(occ_c, 1);
+    ls.grid_shade = sms * std::max(occ_s, 1);
+    ls.grid_small = sms * 8;
+    ls.block = 128;
+    return MCRT_OK;
+}
+
+int adjoint_stream(Workspace& w, const std::vector<JobGPU>& jobs, int64_t total, int max_depth, int bvh_depth,
+                   int64_t path_chunk, float* ga, int na, float* ge, int ne, cudaStream_t st, RunResult& run)
+{
+    int64_t capacity = path_chunk > 0 ? path_chunk : kDefaultQueue;
+    capacity = std::min(capacity, (total + 31) / 32 * 32);
+    capacity = std::max<int64_t>(capacity, 64);
+    WaveArgs a;
+    int      rc = begin_run(w, jobs, capacity, 0, 0, st, run, a);
+    if (rc) return rc;
+    if (w.adj_capacity < capacity)
+    {
+        cudaFree(w.adj_block);
+        w.adj_block = nullptr;
+        w.adj_capacity = 0;
+        CK(cudaMalloc(&w.adj_block, 4 * (32 * static_cast<size_t>(capacity) + 256)));
+        w.adj_capacity = capacity;
+    }
+    Carver c{static_cast<char*>(w.adj_block)};
+    for (int k = 0; k < 2; ++k)
+    {
+        a.qlog[k] = static_cast<uint4*>(c.take(32 * static_cast<size_t>(w.adj_capacity)));
+        a.dlog[k] = static_cast<uint4*>(c.take(32 * static_cast<size_t>(w.adj_capacity)));
+    }
+    a.g_albedo = ga;
+    a.g_emis = ge;
+    a.n_albedo = na;
+    a.n_emis = ne;
+    const size_t gbytes = sizeof(float) * 3 * static_cast<size_t>(na + ne);
+    a.grad_shared = gbytes <= 64 * 1024 ? 1 : 0;
+    const size_t dyn = a.grad_shared ? gbytes : 0;
+    const bool   stack32 = bvh_depth + 2 < 32;
+    LaunchShape  ls;
+    rc = stack32 ? adjoint_launch_shape<32>(dyn, ls) : adjoint_launch_shape<kStack>(dyn, ls);
+    if (rc) return rc;
+    auto iter = [&](cudaStream_t s2, int p, StageTimer*) {
+        if (stack32)
+            enqueue_adjoint_iter<32>(a, p, ls, s2, dyn);
+        else
+            enqueue_adjoint_iter<kStack>(a, p, ls, s2, dyn);
+    };
+    StageTimer timer;
+    return stream_loop(w, a, total, max_depth, false, true, st, timer, run, iter);
 }
 
 int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams, const mcrt_render_params* params,
@@ -1360,21 +1611,6 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
 
 namespace mcrt {
 
-namespace {
-// sub-array allocator: 256-B aligned pieces of one block
-struct Carver
-{
-    char* p;
-    void* take(size_t n)
-    {
-        size_t off = (reinterpret_cast<uintptr_t>(p) + 255) & ~static_cast<uintptr_t>(255);
-        char*  r = reinterpret_cast<char*>(off);
-        p = r + n;
-        return r;
-    }
-};
-}  // namespace
-
 size_t queue_bytes(int64_t capacity)
 {
     const size_t C = static_cast<size_t>(capacity);
@@ -1445,8 +1681,9 @@ LaunchShape launch_shape_variant(bool stack32, bool regcap)
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &occ_t, regcap ? k_extend<kStack, false, 8> : k_extend<kStack, false, 1>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<false>, 128, 0);
     ls.grid_trace = sms * std::max(occ_t, 1);
+    ls.grid_connect = ls.grid_trace;
     ls.grid_shade = sms * std::max(occ_s, 1);
     ls.grid_small = sms * 8;
     ls.block = 128;
@@ -1808,7 +2045,63 @@ static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_came
         dge = static_cast<float*>(a3);
     }
     Workspace& w = owner->ws;
-    int        rc = ensure_workspace(w, 0, 0, num_jobs, 1);
+    // the wavefront replay (default) needs the vertex log to hold every vertex and 16-bit
+    // material ids; otherwise, or with MCRT_SCHEDULE_WAVES, one thread replays each path
+    int  max_depth = 0, bvh_depth = 0;
+    bool small_ids = true;
+    for (int j = 0; j < num_jobs; ++j)
+    {
+        max_depth = std::max(max_depth, params[j].max_depth);
+        bvh_depth = std::max(bvh_depth, scenes[j]->bvh_depth);
+        small_ids = small_ids && scenes[j]->num_materials <= 65536;
+    }
+    if (params[0].schedule == MCRT_SCHEDULE_STREAM && max_depth < kAdjLog && small_ids)
+    {
+        RunResult run;
+        int       rc = adjoint_stream(w, jobs, total, max_depth, bvh_depth, params[0].path_chunk, dga, n_albedo, dge,
+                                      n_emis, st, run);
+        if (rc)
+        {
+            cudaStreamSynchronize(st);
+            cleanup();
+            return rc;
+        }
+        h2d += static_cast<int64_t>(sizeof(JobGPU)) * num_jobs;
+        if (ptr_mode != MCRT_PTR_DEVICE)
+        {
+            if (n_albedo > 0) CK(cudaMemcpyAsync(d_albedo, dga, sizeof(float) * 3 * n_albedo, cudaMemcpyDeviceToHost, st));
+            if (n_emis > 0) CK(cudaMemcpyAsync(d_emis, dge, sizeof(float) * 3 * n_emis, cudaMemcpyDeviceToHost, st));
+            d2h += sizeof(float) * 3 * (n_albedo + n_emis);
+        }
+        unsigned long long hstats[8];
+        int                herr = 0;
+        CK(cudaMemcpyAsync(hstats, w.stats, sizeof(hstats), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&herr, w.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        d2h += sizeof(hstats) + sizeof(herr) + run.poll_bytes;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, run.e0, run.e1);
+        cudaEventDestroy(run.e0);
+        cudaEventDestroy(run.e1);
+        cleanup();
+        if (stats)
+        {
+            *stats = mcrt_render_stats{};
+            stats->paths = total;
+            stats->extension_rays = static_cast<int64_t>(hstats[0]);
+            stats->shadow_rays = static_cast<int64_t>(hstats[1]);
+            stats->waves = static_cast<int32_t>(run.waves);
+            stats->kernel_launches = static_cast<int32_t>(run.launches);
+            stats->extend_launches = static_cast<int32_t>(run.extend_launches);
+            stats->device_ms = ms;
+            stats->h2d_bytes = h2d;
+            stats->d2h_bytes = d2h;
+        }
+        if (herr & kErrStack) return fail(MCRT_ERR_STACK_OVERFLOW, "traversal stack overflow");
+        if (herr & kErrQueue) return fail(MCRT_ERR_QUEUE_OVERFLOW, "queue overflow");
+        return MCRT_OK;
+    }
+    int rc = ensure_workspace(w, 0, 0, num_jobs, 1);
     if (rc)
     {
         cleanup();

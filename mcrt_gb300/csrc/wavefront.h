@@ -73,7 +73,8 @@ struct WaveArgs
     // next-event results by parity: [4 i + s] for queue position i, [4 capacity + 4 j + s]
     // for finished-list position j
     float4* nev[2];
-    // next-event queues: [0] any-hit, [1] closest-hit; meta = {result index, type, light, job}
+    // next-event queues: [0] any-hit, [1] closest-hit; meta = {result index, type | light << 2,
+    // pixel, job}
     float4* so[2];
     float4* sd[2];
     float4* sv[2];
@@ -86,11 +87,37 @@ struct WaveArgs
     int64_t             ring_size;
     unsigned long long* stats;  // [0] extension rays, [1] next-event rays, [2..5] work counters
     int*                err;
+    // adjoint (paths replayed through the same queues, JobGPU::image = dL/dimage): the
+    // material ids of a path's parameterised Lambert vertices, 16 bits each, at most
+    // kAdjLog per path (thr.w bits 20.. hold the count), two uint4 per queue position and
+    // per finished-list position; gradients (in shared memory per block when grad_shared)
+    uint4* qlog[2];
+    uint4* dlog[2];
+    float* g_albedo;
+    float* g_emis;
+    int    n_albedo;
+    int    n_emis;
+    int    grad_shared;
 };
+
+constexpr int kAdjLog = 16;
 
 struct LaunchShape
 {
-    int grid_trace, grid_shade, grid_small, block;
+    int grid_trace, grid_connect, grid_shade, grid_small, block;
+};
+
+// sub-array allocator: consecutive 256-B aligned pieces of one block
+struct Carver
+{
+    char* p;
+    void* take(size_t n)
+    {
+        size_t off = (reinterpret_cast<uintptr_t>(p) + 255) & ~static_cast<uintptr_t>(255);
+        char*  r = reinterpret_cast<char*>(off);
+        p = r + n;
+        return r;
+    }
 };
 
 // bytes of the queues for `capacity` rays (256-B aligned sub-arrays)

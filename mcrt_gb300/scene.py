@@ -219,10 +219,11 @@ class GpuScene:
 
     def render_adjoint(self, camera: CameraDesc, spp: int, max_depth: int, dL_dimage, n_albedo: int,
                        n_emission: int, rr_depth: int = -1, seed: int = 0, traverse: int = N.TRAVERSE_FAST,
-                       d_albedo=None, d_emission=None):
+                       d_albedo=None, d_emission=None, schedule: int = N.SCHEDULE_STREAM, path_chunk: int = 0):
         """Path-replay adjoint; returns (d_albedo (n,3), d_emission (m,3), stats).
-        Gradients are ADDED into d_albedo / d_emission when given."""
-        p = make_params(spp, max_depth, rr_depth, seed, traverse, 0, False)
+        Gradients are ADDED into d_albedo / d_emission when given.  schedule STREAM replays
+        the paths through the wavefront queues; WAVES replays each path in one thread."""
+        p = make_params(spp, max_depth, rr_depth, seed, traverse, path_chunk, False, schedule=schedule)
         cam = camera.to_c()
         st = N.RenderStats()
         if _is_torch(dL_dimage):

@@ -129,3 +129,29 @@ def test_batched_adjoint_equals_sum_of_single_adjoints(cuda_device):
     np.testing.assert_allclose(gab, ga, rtol=1e-4, atol=1e-5)
     np.testing.assert_allclose(geb, ge, rtol=1e-4, atol=1e-5)
     assert st["paths"] == 32 * 32 * 8 + 24 * 20 * 4
+
+
+@pytest.mark.parametrize("path_chunk", [0, 512])
+def test_wavefront_adjoint_equals_per_path_replay(path_chunk, cuda_device):
+    """The wavefront replay (queues, vertex log, split albedo term) and the one-thread-per-
+    path replay compute the same derivative; they differ only in float summation order."""
+    desc, cam, albedo, emission, sc = _setup()
+    rng = np.random.default_rng(8)
+    dl = rng.normal(size=(RES, RES, 3)).astype(np.float32)
+    ga_w, ge_w, st_w = sc.render_adjoint(cam, SPP, DEPTH, dl, albedo.shape[0], 1, seed=4, schedule=0,
+                                         path_chunk=path_chunk)
+    ga_m, ge_m, st_m = sc.render_adjoint(cam, SPP, DEPTH, dl, albedo.shape[0], 1, seed=4, schedule=1)
+    for got, want, name in ((ga_w, ga_m, "albedo"), (ge_w, ge_m, "emission")):
+        err = np.linalg.norm(got - want) / np.linalg.norm(want)
+        assert err < 1e-4, f"{name}: relative L2 difference {err:.3e}"
+    assert st_w["extension_rays"] + st_w["shadow_rays"] == st_m["extension_rays"]
+    if path_chunk:
+        assert st_w["waves"] > 8
+
+
+def test_deep_adjoint_uses_per_path_replay(cuda_device):
+    """Depths beyond the wavefront vertex log replay each path in one thread."""
+    desc, cam, albedo, emission, sc = _setup()
+    dl = np.ones((RES, RES, 3), np.float32)
+    ga, ge, st = sc.render_adjoint(cam, 2, 20, dl, albedo.shape[0], 1, seed=4)
+    assert st["waves"] == 1 and np.all(np.isfinite(ga)) and np.abs(ga).sum() > 0
