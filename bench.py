@@ -267,6 +267,7 @@ def main():
     ap.add_argument("--schedule", default="stream", choices=["stream", "waves"],
                     help="stream: slots refilled with new paths as paths end; waves: fixed waves")
     ap.add_argument("--path-chunk", type=int, default=0, help="path slots in flight (0: library default)")
+    ap.add_argument("--variant", type=int, default=0, help="traversal kernel variant bits (0: default policy)")
     args = ap.parse_args()
     args.schedule_id = 0 if args.schedule == "stream" else 1
     if args.impl == "reference":
@@ -308,7 +309,7 @@ def main():
     out = torch.empty((cam.height, cam.width, 3), dtype=torch.float32, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
     kw = dict(spp=p["spp"], max_depth=p["max_depth"], rr_depth=p["rr_depth"], traverse=traverse,
-              schedule=args.schedule_id, path_chunk=args.path_chunk)
+              schedule=args.schedule_id, path_chunk=args.path_chunk, variant=args.variant)
 
     def barrier():
         if dist:
@@ -405,7 +406,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scene, seeded)",
             "config": {"workload": text, "traversal": args.traverse, "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"replicas x{world}", "schedule": args.schedule,
-                       "path_slots": args.path_chunk or "default",
+                       "path_slots": args.path_chunk or "default", "variant": args.variant,
                        "waves_or_iterations_per_step": st_last["waves"],
                        "scene_setup_s": round(setup_s, 2)},
             "msamples_per_s": round(msamples, 3),

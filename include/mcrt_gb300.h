@@ -160,6 +160,7 @@ typedef struct mcrt_render_params {
 #define MCRT_VARIANT_REGCAP 2   /* cap registers at 64 so 8 blocks of 128 threads fit an SM */
 #define MCRT_VARIANT_EXPLICIT 4 /* use the bits as given instead of the default policy */
 
+
 #define MCRT_PROFILE_STAGES 1 /* CUDA events around every stage launch -> stats.stage_ms */
 #define MCRT_PROFILE_COUNT 2  /* count BVH nodes fetched / triangles tested per ray class */
 

@@ -170,102 +170,131 @@ struct TraceCount
 
 // Two-child traversal over FastNode with a per-thread stack in shared memory
 // (`stack` points at this thread's column, entries `stride` ints apart), nearer child
-// first.  (Postponing leaves until the whole warp holds one, Aila & Laine 2009, measured
-// slower on this GPU: 178 vs 132 ms of closest-hit traversal per cfg1 frame.)
+// first.  FastTrav holds the traversal state; fast_step descends to the next leaf, tests
+// its triangles and pops.  Measured alternatives on this GPU (cfg1 frame, closest-hit
+// traversal time): postponing leaves until the whole warp holds one (Aila & Laine 2009)
+// 178 vs 132 ms; persistent lanes that take a new ray from the queue when 1-16 lanes of
+// the warp are idle 153-161 vs 82 ms -- a ray pulled into a warp mid-traversal shares no
+// nodes with its neighbours, and consecutive queue entries (neighbouring paths) do.
+struct FastTrav
+{
+    float3        inv, ood;
+    WatertightRay wr;
+    float         tmin, best;
+    Hit           hit;
+    int           sp, cur;
+};
+
+__device__ __forceinline__ void fast_begin(FastTrav& r, float3 o, float3 d, float tmin, float tmax, int* stack)
+{
+    const float big = 1e30f;
+    r.inv = mk(fabsf(d.x) > 1e-30f ? 1.0f / d.x : copysignf(big, d.x),
+               fabsf(d.y) > 1e-30f ? 1.0f / d.y : copysignf(big, d.y),
+               fabsf(d.z) > 1e-30f ? 1.0f / d.z : copysignf(big, d.z));
+    r.ood = o * r.inv;
+    r.wr = make_wray(o, d);
+    r.tmin = tmin;
+    r.best = tmax;
+    r.hit.prim = -1;
+    r.sp = 0;
+    stack[0] = kSentinel;
+    r.cur = 0;
+}
+
+// Inner nodes down to the next leaf, that leaf's triangles, then the next node from the
+// stack.  Returns true when the traversal is over: stack empty, an any-hit query hit,
+// or the stack overflowed (error bit set, the hit so far kept).
+template <int STACK, bool COUNT>
+__device__ __forceinline__ bool fast_step(FastTrav& r, const FastNode* nodes, const float4* tris, bool any, int* stack,
+                                          int stride, int* err, TraceCount* cnt)
+{
+    while (r.cur >= 0 && r.cur != kSentinel)
+    {
+        const float4* np = reinterpret_cast<const float4*>(nodes + r.cur);
+        if (COUNT) cnt->nodes++;
+        float4 n0 = __ldg(np + 0);
+        float4 n1 = __ldg(np + 1);
+        float4 n2 = __ldg(np + 2);
+        int4   n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+        float  c0lx = n0.x * r.inv.x - r.ood.x, c0hx = n0.y * r.inv.x - r.ood.x;
+        float  c0ly = n0.z * r.inv.y - r.ood.y, c0hy = n0.w * r.inv.y - r.ood.y;
+        float  c0lz = n2.x * r.inv.z - r.ood.z, c0hz = n2.y * r.inv.z - r.ood.z;
+        float  c1lx = n1.x * r.inv.x - r.ood.x, c1hx = n1.y * r.inv.x - r.ood.x;
+        float  c1ly = n1.z * r.inv.y - r.ood.y, c1hy = n1.w * r.inv.y - r.ood.y;
+        float  c1lz = n2.z * r.inv.z - r.ood.z, c1hz = n2.w * r.inv.z - r.ood.z;
+        float  t0n = fmaxf(fmaxf(fminf(c0lx, c0hx), fminf(c0ly, c0hy)), fmaxf(fminf(c0lz, c0hz), r.tmin));
+        float  t0f = fminf(fminf(fmaxf(c0lx, c0hx), fmaxf(c0ly, c0hy)), fminf(fmaxf(c0lz, c0hz), r.best));
+        float  t1n = fmaxf(fmaxf(fminf(c1lx, c1hx), fminf(c1ly, c1hy)), fmaxf(fminf(c1lz, c1hz), r.tmin));
+        float  t1f = fminf(fminf(fmaxf(c1lx, c1hx), fmaxf(c1ly, c1hy)), fminf(fmaxf(c1lz, c1hz), r.best));
+        // widen the far bound by a few ulp so boxes flat in one axis are not lost
+        bool h0 = t0n <= t0f * 1.0000004f + 1e-30f;
+        bool h1 = t1n <= t1f * 1.0000004f + 1e-30f;
+        if (!h0 && !h1)
+        {
+            r.cur = stack[r.sp * stride];
+            --r.sp;
+        }
+        else
+        {
+            int near = h0 ? n3.x : n3.y;
+            if (h0 && h1)
+            {
+                int far = n3.y;
+                if (t1n < t0n)
+                {
+                    near = n3.y;
+                    far = n3.x;
+                }
+                ++r.sp;
+                if (r.sp >= STACK)
+                {
+                    atomicOr(err, kErrStack);
+                    return true;
+                }
+                stack[r.sp * stride] = far;
+            }
+            r.cur = near;
+        }
+    }
+    if (r.cur < 0)
+    {
+        int code = ~r.cur;
+        int first = code >> 4, count = code & 15;
+        if (COUNT) cnt->tris += count;
+        for (int k = 0; k < count; ++k)
+        {
+            const float4* tp = tris + 3 * (first + k);
+            float4        a = __ldg(tp + 0);
+            float4        b = __ldg(tp + 1);
+            float4        c = __ldg(tp + 2);
+            float         t, u, v;
+            if (watertight(r.wr, xyz(a), xyz(b), xyz(c), r.tmin, r.best, t, u, v))
+            {
+                r.best = t;
+                r.hit.t = t;
+                r.hit.u = u;
+                r.hit.v = v;
+                r.hit.prim = __float_as_int(a.w);
+                if (any) return true;
+            }
+        }
+        r.cur = stack[r.sp * stride];
+        --r.sp;
+    }
+    return r.cur == kSentinel;
+}
+
 template <bool ANY, int STACK, bool COUNT = false>
 __device__ __forceinline__ bool trace_fast(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
                                            int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr)
 {
-    const float big = 1e30f;
-    float3      inv = mk(fabsf(d.x) > 1e-30f ? 1.0f / d.x : copysignf(big, d.x),
-                         fabsf(d.y) > 1e-30f ? 1.0f / d.y : copysignf(big, d.y),
-                         fabsf(d.z) > 1e-30f ? 1.0f / d.z : copysignf(big, d.z));
-    float3      ood = o * inv;
-    WatertightRay wr = make_wray(o, d);
-    hit.prim = -1;
-    float best = tmax;
-    int   sp = 0;
-    stack[0] = kSentinel;
-    int cur = 0;
-    while (cur != kSentinel)
+    FastTrav r;
+    fast_begin(r, o, d, tmin, tmax, stack);
+    while (!fast_step<STACK, COUNT>(r, s.fast_nodes, s.fast_tris, ANY, stack, stride, err, cnt))
     {
-        // inner nodes
-        while (cur >= 0 && cur != kSentinel)
-        {
-            const float4* np = reinterpret_cast<const float4*>(s.fast_nodes + cur);
-            if (COUNT) cnt->nodes++;
-            float4        n0 = __ldg(np + 0);
-            float4        n1 = __ldg(np + 1);
-            float4        n2 = __ldg(np + 2);
-            int4          n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
-            float c0lx = n0.x * inv.x - ood.x, c0hx = n0.y * inv.x - ood.x;
-            float c0ly = n0.z * inv.y - ood.y, c0hy = n0.w * inv.y - ood.y;
-            float c0lz = n2.x * inv.z - ood.z, c0hz = n2.y * inv.z - ood.z;
-            float c1lx = n1.x * inv.x - ood.x, c1hx = n1.y * inv.x - ood.x;
-            float c1ly = n1.z * inv.y - ood.y, c1hy = n1.w * inv.y - ood.y;
-            float c1lz = n2.z * inv.z - ood.z, c1hz = n2.w * inv.z - ood.z;
-            float t0n = fmaxf(fmaxf(fminf(c0lx, c0hx), fminf(c0ly, c0hy)), fmaxf(fminf(c0lz, c0hz), tmin));
-            float t0f = fminf(fminf(fmaxf(c0lx, c0hx), fmaxf(c0ly, c0hy)), fminf(fmaxf(c0lz, c0hz), best));
-            float t1n = fmaxf(fmaxf(fminf(c1lx, c1hx), fminf(c1ly, c1hy)), fmaxf(fminf(c1lz, c1hz), tmin));
-            float t1f = fminf(fminf(fmaxf(c1lx, c1hx), fmaxf(c1ly, c1hy)), fminf(fmaxf(c1lz, c1hz), best));
-            // widen the far bound by a few ulp so boxes flat in one axis are not lost
-            bool h0 = t0n <= t0f * 1.0000004f + 1e-30f;
-            bool h1 = t1n <= t1f * 1.0000004f + 1e-30f;
-            if (!h0 && !h1)
-            {
-                cur = stack[sp * stride];
-                --sp;
-            }
-            else
-            {
-                int near = h0 ? n3.x : n3.y;
-                if (h0 && h1)
-                {
-                    int far = n3.y;
-                    if (t1n < t0n)
-                    {
-                        near = n3.y;
-                        far = n3.x;
-                    }
-                    ++sp;
-                    if (sp >= STACK)
-                    {
-                        atomicOr(err, kErrStack);
-                        return hit.prim >= 0;
-                    }
-                    stack[sp * stride] = far;
-                }
-                cur = near;
-            }
-        }
-        // leaves
-        while (cur < 0)
-        {
-            int code = ~cur;
-            int first = code >> 4, count = code & 15;
-            if (COUNT) cnt->tris += count;
-            for (int k = 0; k < count; ++k)
-            {
-                const float4* tp = s.fast_tris + 3 * (first + k);
-                float4        a = __ldg(tp + 0);
-                float4        b = __ldg(tp + 1);
-                float4        c = __ldg(tp + 2);
-                float         t, u, v;
-                if (watertight(wr, xyz(a), xyz(b), xyz(c), tmin, best, t, u, v))
-                {
-                    best = t;
-                    hit.t = t;
-                    hit.u = u;
-                    hit.v = v;
-                    hit.prim = __float_as_int(a.w);
-                    if (ANY) return true;
-                }
-            }
-            cur = stack[sp * stride];
-            --sp;
-        }
     }
-    return hit.prim >= 0;
+    hit = r.hit;
+    return r.hit.prim >= 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -413,26 +442,28 @@ __device__ __forceinline__ bool trace_ref(const SceneView& s, float3 o, float3 d
     return hit.prim >= 0;
 }
 
+// The watertight test decides which triangle is closest; the reported t, u, v of that
+// one triangle are then recomputed with the reference's Moller-Trumbore arithmetic (each
+// formula lands ~3 ulp from the exact t, on either side).
+__device__ __forceinline__ void refine_hit(const SceneView& s, float3 o, float3 d, float tmin, Hit& hit)
+{
+    const float4* pv = s.prim_verts + 3 * hit.prim;
+    float         t, u, v;
+    if (ref_mt(o, d, xyz(__ldg(pv)), xyz(__ldg(pv + 1)), xyz(__ldg(pv + 2)), t, u, v) && t > tmin)
+    {
+        hit.t = t;
+        hit.u = u;
+        hit.v = v;
+    }
+}
+
 template <bool ANY, int STACK, bool COUNT = false>
 __device__ __forceinline__ bool trace_ray(const SceneView& s, int mode, float3 o, float3 d, float tmin, float tmax,
                                           int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr)
 {
     if (mode == 1) return trace_ref<ANY, STACK>(s, o, d, tmin, tmax, stack, stride, hit, err);
     bool found = trace_fast<ANY, STACK, COUNT>(s, o, d, tmin, tmax, stack, stride, hit, err, cnt);
-    if (!ANY && found)
-    {
-        // The watertight test decides which triangle is closest; the reported t, u, v
-        // of that one triangle are then recomputed with the reference's Moller-Trumbore
-        // arithmetic (each formula lands ~3 ulp from the exact t, on either side).
-        const float4* pv = s.prim_verts + 3 * hit.prim;
-        float         t, u, v;
-        if (ref_mt(o, d, xyz(__ldg(pv)), xyz(__ldg(pv + 1)), xyz(__ldg(pv + 2)), t, u, v) && t > tmin)
-        {
-            hit.t = t;
-            hit.u = u;
-            hit.v = v;
-        }
-    }
+    if (!ANY && found) refine_hit(s, o, d, tmin, hit);
     return found;
 }
 

@@ -414,12 +414,18 @@ __global__ void __launch_bounds__(128) k_regen(WaveArgs a, int p)
     grads_end<ADJ>(a, sgrad);
 }
 
+__device__ __forceinline__ float4 hit_record(bool hit, const Hit& h)
+{
+    return hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.prim)) : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+}
+
 template <int STACK, bool COUNT, int MINB>
 __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
 {
     __shared__ int stack[STACK * kTraceBlock];
     int*           st = stack + threadIdx.x;
     const int      n = min(a.ctrl->qcount[p], static_cast<int>(a.capacity));
+    const float    inf = __int_as_float(0x7f800000);
     TraceCount     cnt = {0u, 0u};
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[0], static_cast<unsigned long long>(n));
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -427,10 +433,9 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
         float4        o = a.qo[p][i], d = a.qd[p][i];
         const JobGPU& J = a.jobs[__float_as_int(o.w)];
         Hit           h;
-        bool hit = trace_ray<false, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), kEpsRay,
-                                                  __int_as_float(0x7f800000), st, kTraceBlock, h, a.err, &cnt);
-        a.hits[i] = hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.prim))
-                        : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+        bool hit = trace_ray<false, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), kEpsRay, inf, st, kTraceBlock, h,
+                                                  a.err, &cnt);
+        a.hits[i] = hit_record(hit, h);
     }
     if (COUNT) flush_count(a.stats, 2, cnt);
 }
@@ -630,6 +635,27 @@ __global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
 
 // Adjoint (ADJ): the emission derivative of each next-event contribution (the
 // coefficient of the reached emitter's E)
+template <bool ADJ>
+__device__ __forceinline__ void connect_result(const WaveArgs& a, const Grads& G, int p, int n0, int i, bool hit,
+                                               const Hit& h)
+{
+    const int        q = i < n0 ? 0 : 1;
+    const int        k = i < n0 ? i : i - n0;
+    const float4     d = a.sd[q][k], v = a.sv[q][k];
+    const int4       m = a.sm[q][k];
+    const JobGPU&    J = a.jobs[m.w];
+    const SceneView& S = J.scene;
+    float3           coef;
+    int              emat;
+    float3           add = nee_contribution(S, m.y & 3, m.y >> 2, v, xyz(d), hit, h, coef, emat);
+    a.nev[p ^ 1][m.x] = make_float4(add.x, add.y, add.z, 0.f);
+    if (ADJ && emat >= 0)
+    {
+        const int ep = S.materials[emat].emission_param;
+        if (ep >= 0 && ep < a.n_emis) add_grad3(G.ge, ep, coef * path_dl(J, m.z));
+    }
+}
+
 template <int STACK, bool COUNT, int MINB, bool ADJ>
 __global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, int p)
 {
@@ -640,30 +666,19 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, int p
     TraceCount     cnt = {0u, 0u};
     const int      n0 = min(a.ctrl->scount[0], static_cast<int>(a.shadow_cap));
     const int      n1 = min(a.ctrl->scount[1], static_cast<int>(a.shadow_cap));
-    float4*        res = a.nev[p ^ 1];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[1], static_cast<unsigned long long>(n0 + n1));
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0 + n1; i += gridDim.x * blockDim.x)
     {
-        int              q = i < n0 ? 0 : 1;
-        int              k = i < n0 ? i : i - n0;
-        float4           o = a.so[q][k], d = a.sd[q][k], v = a.sv[q][k];
-        int4             m = a.sm[q][k];
-        const JobGPU&    J = a.jobs[m.w];
-        const SceneView& S = J.scene;
-        Hit              h;
-        bool hit = q == 0 ? trace_ray<true, STACK, COUNT>(S, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock, h,
-                                                          a.err, &cnt)
-                          : trace_ray<false, STACK, COUNT>(S, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock,
-                                                           h, a.err, &cnt);
-        float3 coef;
-        int    emat;
-        float3 add = nee_contribution(S, m.y & 3, m.y >> 2, v, xyz(d), hit, h, coef, emat);
-        res[m.x] = make_float4(add.x, add.y, add.z, 0.f);
-        if (ADJ && emat >= 0)
-        {
-            const int ep = S.materials[emat].emission_param;
-            if (ep >= 0 && ep < a.n_emis) add_grad3(G.ge, ep, coef * path_dl(J, m.z));
-        }
+        int           q = i < n0 ? 0 : 1;
+        int           k = i < n0 ? i : i - n0;
+        float4        o = a.so[q][k], d = a.sd[q][k];
+        const JobGPU& J = a.jobs[a.sm[q][k].w];
+        Hit           h;
+        bool hit = q == 0 ? trace_ray<true, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock,
+                                                          h, a.err, &cnt)
+                          : trace_ray<false, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st,
+                                                           kTraceBlock, h, a.err, &cnt);
+        connect_result<ADJ>(a, G, p, n0, i, hit, h);
     }
     if (COUNT) flush_count(a.stats, 4, cnt);
     grads_end<ADJ>(a, sgrad);
