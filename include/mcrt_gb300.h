@@ -159,6 +159,8 @@ typedef struct mcrt_render_params {
 #define MCRT_VARIANT_STACK32 1  /* 32-entry shared-memory stacks (16 KB/block) when the BVH is shallow enough */
 #define MCRT_VARIANT_REGCAP 2   /* cap registers at 64 so 8 blocks of 128 threads fit an SM */
 #define MCRT_VARIANT_EXPLICIT 4 /* use the bits as given instead of the default policy */
+#define MCRT_VARIANT_GRIDSTRIDE 8 /* traversal kernels: static grid stride instead of warps taking
+                                     32-ray batches from a counter */
 
 
 #define MCRT_PROFILE_STAGES 1 /* CUDA events around every stage launch -> stats.stage_ms */

@@ -32,6 +32,7 @@ PROFILE_COUNT = 2
 VARIANT_STACK32 = 1
 VARIANT_REGCAP = 2
 VARIANT_EXPLICIT = 4
+VARIANT_GRIDSTRIDE = 8
 SCHEDULE_STREAM = 0
 SCHEDULE_WAVES = 1
 BUILD_SAH = 0

@@ -141,6 +141,7 @@ __global__ void k_render_begin(WaveArgs a, int waves, int64_t limit)
     c->scount[0] = c->scount[1] = 0;
     c->new_base = c->new_count = 0;
     c->chunk = -1;
+    c->fetch[0] = c->fetch[1] = 0;
     c->pad = 0;
     c->next = 0;
     c->limit = waves ? 0ull : static_cast<unsigned long long>(limit);
@@ -163,6 +164,8 @@ __global__ void k_iter_begin(WaveArgs a, int p)
     c->dcount[p ^ 1] = 0;
     c->scount[0] = 0;
     c->scount[1] = 0;
+    c->fetch[0] = 0;
+    c->fetch[1] = 0;
     // top the queue up with new paths (continuing rays are already in it)
     const int                q = c->qcount[p];
     const unsigned long long avail = c->limit > c->next ? c->limit - c->next : 0ull;
@@ -414,6 +417,41 @@ __global__ void __launch_bounds__(128) k_regen(WaveArgs a, int p)
     grads_end<ADJ>(a, sgrad);
 }
 
+// Work distribution of the traversal kernels over a queue of n entries: with batch
+// fetch each warp takes the next 32 consecutive entries from `counter` until the queue is
+// exhausted (the launch ends within one batch of its slowest warp; consecutive entries
+// are neighbouring paths, so a warp's rays stay coherent); otherwise a static grid
+// stride.  Usage: for (QueueWalk w(...); w.valid(); w.next()) if (w.i < n) ...
+struct QueueWalk
+{
+    int* counter;
+    int  n, i, base;
+    bool batch;
+    __device__ __forceinline__ QueueWalk(int* c, int n_, bool batch_) : counter(c), n(n_), batch(batch_)
+    {
+        if (batch)
+            fetch();
+        else
+            base = i = blockIdx.x * blockDim.x + threadIdx.x;
+    }
+    __device__ __forceinline__ void fetch()
+    {
+        int b = 0;
+        if ((threadIdx.x & 31) == 0) b = atomicAdd(counter, 32);
+        base = __shfl_sync(0xffffffffu, b, 0);
+        i = base + (threadIdx.x & 31);
+    }
+    // batch: warp-uniform (the whole warp continues while its batch starts inside the queue)
+    __device__ __forceinline__ bool valid() const { return batch ? base < n : i < n; }
+    __device__ __forceinline__ void next()
+    {
+        if (batch)
+            fetch();
+        else
+            base = i += gridDim.x * blockDim.x;
+    }
+};
+
 __device__ __forceinline__ float4 hit_record(bool hit, const Hit& h)
 {
     return hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.prim)) : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
@@ -428,8 +466,10 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
     const float    inf = __int_as_float(0x7f800000);
     TraceCount     cnt = {0u, 0u};
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[0], static_cast<unsigned long long>(n));
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (QueueWalk w(&a.ctrl->fetch[0], n, a.batch_fetch != 0); w.valid(); w.next())
     {
+        const int i = w.i;
+        if (i >= n) continue;
         float4        o = a.qo[p][i], d = a.qd[p][i];
         const JobGPU& J = a.jobs[__float_as_int(o.w)];
         Hit           h;
@@ -667,8 +707,10 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, int p
     const int      n0 = min(a.ctrl->scount[0], static_cast<int>(a.shadow_cap));
     const int      n1 = min(a.ctrl->scount[1], static_cast<int>(a.shadow_cap));
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[1], static_cast<unsigned long long>(n0 + n1));
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0 + n1; i += gridDim.x * blockDim.x)
+    for (QueueWalk w(&a.ctrl->fetch[1], n0 + n1, a.batch_fetch != 0); w.valid(); w.next())
     {
+        const int i = w.i;
+        if (i >= n0 + n1) continue;
         int           q = i < n0 ? 0 : 1;
         int           k = i < n0 ? i : i - n0;
         float4        o = a.so[q][k], d = a.sd[q][k];
@@ -1566,6 +1608,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     const bool  regcap = (vb & MCRT_VARIANT_REGCAP) != 0;
     LaunchShape lsv = launch_shape_variant(stack32, regcap);
     Workspace&  w = owner->ws;
+    w.args.batch_fetch = (vb & MCRT_VARIANT_GRIDSTRIDE) ? 0 : 1;
     StageTimer  timer;
     RunResult   run;
     int         rc = p0.schedule == MCRT_SCHEDULE_WAVES
@@ -2072,6 +2115,7 @@ static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_came
     }
     if (params[0].schedule == MCRT_SCHEDULE_STREAM && max_depth < kAdjLog && small_ids)
     {
+        w.args.batch_fetch = 1;
         RunResult run;
         int       rc = adjoint_stream(w, jobs, total, max_depth, bvh_depth, params[0].path_chunk, dga, n_albedo, dge,
                                       n_emis, st, run);

@@ -156,6 +156,7 @@ extern "C" int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera,
         a.num_jobs = 1;
         a.stats = L.stats;
         a.err = L.err;
+        a.batch_fetch = 1;
         // the array keeps the previous call's contents: clear what must start at zero
         e = cudaMemsetAsync(L.stats, 0, 8 * sizeof(unsigned long long), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(L.err, 0, sizeof(int), st);

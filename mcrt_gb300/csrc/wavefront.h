@@ -43,6 +43,7 @@ struct Ctrl
     int                new_base;   // this iteration's admitted paths: first queue position
     int                new_count;  //   and how many
     int                chunk;      // wave schedule: index of the current wave
+    int                fetch[2];   // rays taken so far by this iteration's k_extend, k_connect warps
     int                pad;
     unsigned long long next;      // index of the next path to admit
     unsigned long long limit;     // admission limit (exclusive)
@@ -87,6 +88,9 @@ struct WaveArgs
     int64_t             ring_size;
     unsigned long long* stats;  // [0] extension rays, [1] next-event rays, [2..5] work counters
     int*                err;
+    // traversal kernels: each warp takes the next 32 queue entries from a counter until the
+    // queue is empty (1), or every thread strides over the queue by the grid size (0)
+    int batch_fetch;
     // adjoint (paths replayed through the same queues, JobGPU::image = dL/dimage): the
     // material ids of a path's parameterised Lambert vertices, 16 bits each, at most
     // kAdjLog per path (thr.w bits 20.. hold the count), two uint4 per queue position and
