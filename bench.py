@@ -185,12 +185,19 @@ def bench_cfg2(args):
             tot += st["rays"]
         return tot
     ts, seq_rays = _timed(sequential, reps=args.steps)
+
+    def sequential_waves():
+        for s, c, (_, _, p), o in zip(gs, cams, jobs, outs):
+            s.render(c, out=o, schedule=1, **p)
+    sequential_waves()
+    tw, _ = _timed(sequential_waves, reps=args.steps)
     paths = stb["paths"]
     line = {"workload": "cfg2: 64 scenes, displaced icospheres 1k-500k T in Cornell shells, res {128..1024}^2, "
                         "spp 1..64, depth 4..16", "paths": paths, "rays": stb["rays"],
             "batched_ms": round(tb * 1e3, 2), "sequential_ms": round(ts * 1e3, 2),
             "batched_mrays_s": round(stb["rays"] / tb / 1e6, 1), "sequential_mrays_s": round(seq_rays / ts / 1e6, 1),
             "batched_msamples_s": round(paths / tb / 1e6, 1), "speedup_batched_vs_sequential": round(ts / tb, 3),
+            "sequential_waves_ms": round(tw * 1e3, 2), "speedup_batched_vs_sequential_waves": round(tw / tb, 3),
             "schedule": args.schedule, "waves": stb["waves"], "scene_setup_s": round(setup_s, 1), "triangles": int(sum(d.num_triangles
                                                                                                for d, _, _ in jobs))}
     print(json.dumps(line), flush=True)
@@ -408,7 +415,7 @@ def main():
                        "parallelism": f"replicas x{world}", "schedule": args.schedule,
                        "path_slots": args.path_chunk or "default", "variant": args.variant,
                        "waves_or_iterations_per_step": st_last["waves"],
-                       "scene_setup_s": round(setup_s, 2)},
+                       "scene_setup_s": round(setup_s, 2), "scene_device_bytes": sc.info()["device_bytes"], "fast_nodes": sc.info()["fast_nodes"]},
             "msamples_per_s": round(msamples, 3),
             "rays_per_path": round(rays / max(paths, 1), 3),
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
@@ -421,7 +428,7 @@ def main():
                          "second_kernel": {"kernel": other, "achieved": round(other_achieved, 1),
                                            "frac": round(other_achieved / peak, 4),
                                            "share_of_step": round(oms / max(total_ms, 1e-9), 3)}},
-            "stage_ms_per_step": {"raygen+resolve": round(st_last["stage_ms"][0], 2),
+            "stage_ms_per_step": {"begin+regen": round(st_last["stage_ms"][0], 2),
                                   "extend": round(st_last["stage_ms"][1], 2), "shade": round(st_last["stage_ms"][2], 2),
                                   "connect": round(st_last["stage_ms"][3], 2)},
             "cpu_baseline": cpu,
