@@ -14,9 +14,10 @@
  *   SceneBVH::occluded            src/core/scenebvh.h:18, scenebvh.cpp:379-396 -> mcrt_trace_any
  *   SceneBVH::~SceneBVH           src/core/scenebvh.cpp:398-402                -> mcrt_scene_destroy
  *   rayTrace + DemoSimple::run    src/examples/pt/demo_pt.cpp:512-720        -> mcrt_render
- *   (no reference counterpart: path-replay adjoint, batched launch)           -> mcrt_render_adjoint,
+ *   (no reference counterpart: path-replay adjoint, batched launch, tuning)   -> mcrt_render_adjoint,
  *                                                                                mcrt_render_adjoint_batch,
- *                                                                                mcrt_render_batch
+ *                                                                                mcrt_render_batch,
+ *                                                                                mcrt_autotune
  */
 #ifndef MCRT_GB300_H
 #define MCRT_GB300_H
@@ -231,6 +232,28 @@ int mcrt_render_adjoint_batch(int32_t num_jobs, mcrt_scene* const* scenes, const
 int mcrt_render_batch(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cameras,
                       const mcrt_render_params* params, float* const* rgb_out, mcrt_render_stats* stats,
                       void* stream);
+
+/* Autotuner (no reference counterpart).  Renders a reduced-spp probe of the jobs (the
+ * same scenes, cameras and depths; about 4 queue capacities of paths in total) under
+ * candidate launch configurations -- traversal kernel variants (stack depth, register
+ * cap, work distribution) first, then queue capacities (path_chunk) with the best
+ * variant -- times each by CUDA events (best of two) and writes the fastest to
+ * tuned[0..num_jobs-1] (params with path_chunk and variant set, MCRT_VARIANT_EXPLICIT).
+ * Every candidate renders the same image, so tuning never changes results.  report may
+ * be NULL.  Allocates scratch images on the device; not for use inside a graph capture. */
+#define MCRT_TUNE_MAX 16
+typedef struct mcrt_tune_report {
+    int32_t num_candidates;
+    int32_t chosen;             /* index of the configuration written to tuned */
+    int64_t probe_paths;        /* paths of one probe render */
+    int64_t path_chunk[MCRT_TUNE_MAX];
+    int32_t variant[MCRT_TUNE_MAX];
+    float   ms[MCRT_TUNE_MAX];  /* kernel time of the probe render */
+} mcrt_tune_report;
+
+int mcrt_autotune(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cameras,
+                  const mcrt_render_params* params, mcrt_render_params* tuned, mcrt_tune_report* report,
+                  void* stream);
 
 /* Forward render that allocates nothing (no reference counterpart: MCRT has no GPU and no
  * allocation constraints).  For callers that cannot call cudaMalloc while rendering --

@@ -6,6 +6,8 @@ Public surface:
                                        render_adjoint / set_materials
   render_batch                         many scenes/cameras/spp budgets in one wavefront
   render_adjoint_batch                 the adjoint of render_batch in one launch
+  autotune                             launch configuration (queue capacity, kernel variant)
+                                       timed on a reduced-spp probe of the jobs
   build()                              compile the in-tree native library
 The native library (mcrt_gb300/_lib/libmcrt_gb300.so, C ABI in include/mcrt_gb300.h)
 is required: there is no CPU fallback.
@@ -13,10 +15,11 @@ is required: there is no CPU fallback.
 from . import scenes
 from ._native import (PTR_DEVICE, PTR_HOST, TRAVERSE_FAST, TRAVERSE_REF, McrtError, load)
 from .native_build import build
-from .scene import (DIFF, GGX, GLSY, LGHT, REFR, SPEC, CameraDesc, GpuScene, Material, SceneDesc, make_params,
-                    render_adjoint_batch, render_batch)
+from .scene import (DIFF, GGX, GLSY, LGHT, REFR, SPEC, CameraDesc, GpuScene, Material, SceneDesc, autotune,
+                    make_params, render_adjoint_batch, render_batch)
 
-__all__ = ["SceneDesc", "Material", "CameraDesc", "GpuScene", "render_batch", "render_adjoint_batch", "build", "load",
+__all__ = ["SceneDesc", "Material", "CameraDesc", "GpuScene", "render_batch", "render_adjoint_batch", "autotune",
+           "build", "load",
            "scenes",
            "McrtError", "TRAVERSE_FAST", "TRAVERSE_REF", "PTR_HOST", "PTR_DEVICE", "make_params",
            "LGHT", "DIFF", "SPEC", "REFR", "GLSY", "GGX"]

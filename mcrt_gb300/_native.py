@@ -83,6 +83,14 @@ class RenderStats(ctypes.Structure):
                 ("nee_tris", c_int64), ("h2d_bytes", c_int64), ("d2h_bytes", c_int64)]
 
 
+TUNE_MAX = 16
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("num_candidates", c_int32), ("chosen", c_int32), ("probe_paths", c_int64),
+                ("path_chunk", c_int64 * TUNE_MAX), ("variant", c_int32 * TUNE_MAX), ("ms", c_float * TUNE_MAX)]
+
+
 EXPORTS = {
     "mcrt_get_abi_version": (c_int32, []),
     "mcrt_last_error": (ctypes.c_char_p, []),
@@ -105,6 +113,9 @@ EXPORTS = {
     "mcrt_render_batch": (c_int32, [c_int32, ctypes.POINTER(c_void_p), ctypes.POINTER(Camera),
                                     ctypes.POINTER(RenderParams), ctypes.POINTER(c_void_p),
                                     ctypes.POINTER(RenderStats), c_void_p]),
+    "mcrt_autotune": (c_int32, [c_int32, ctypes.POINTER(c_void_p), ctypes.POINTER(Camera),
+                                ctypes.POINTER(RenderParams), ctypes.POINTER(RenderParams),
+                                ctypes.POINTER(TuneReport), c_void_p]),
 }
 
 _lib = None

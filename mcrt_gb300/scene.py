@@ -298,6 +298,25 @@ def render_batch(scenes: list, cameras: list, params: list, outs: list | None = 
     return outs, stats_dict(st)
 
 
+def autotune(scenes: list, cameras: list, params: list):
+    """mcrt_autotune over (scene, camera, params) jobs.  Returns (tuned params dicts with
+    path_chunk and variant set, report dict with every timed candidate)."""
+    lib = N.load()
+    n = len(scenes)
+    hs = (ctypes.c_void_p * n)(*[s.handle.value for s in scenes])
+    cs = (N.Camera * n)(*[c.to_c() for c in cameras])
+    ps = (N.RenderParams * n)(*[make_params(**p) for p in params])
+    out = (N.RenderParams * n)()
+    rep = N.TuneReport()
+    N.check(lib.mcrt_autotune(n, hs, cs, ps, out, ctypes.byref(rep), None), "mcrt_autotune")
+    tuned = [dict(p, path_chunk=int(out[k].path_chunk), variant=int(out[k].variant)) for k, p in enumerate(params)]
+    k = rep.num_candidates
+    report = {"probe_paths": int(rep.probe_paths), "chosen": int(rep.chosen),
+              "candidates": [{"path_chunk": int(rep.path_chunk[i]), "variant": int(rep.variant[i]),
+                              "ms": round(float(rep.ms[i]), 3)} for i in range(k)]}
+    return tuned, report
+
+
 def render_adjoint_batch(scenes: list, cameras: list, params: list, dL_dimages: list, n_albedo: int,
                          n_emission: int):
     """Adjoint of render_batch: all jobs' paths replayed in one launch, gradients summed.

@@ -66,7 +66,7 @@ def test_struct_layouts_match_header(tmp_path):
     from mcrt_gb300 import _native as N
     pairs = {"mcrt_material": N.Material, "mcrt_bvh_tree": N.BvhTree, "mcrt_scene_desc": N.SceneDesc,
              "mcrt_ray": N.Ray, "mcrt_hit": N.Hit, "mcrt_camera": N.Camera, "mcrt_render_params": N.RenderParams,
-             "mcrt_render_stats": N.RenderStats}
+             "mcrt_render_stats": N.RenderStats, "mcrt_tune_report": N.TuneReport}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "mcrt_gb300.h"', "int main(void) {"]
     for cname, py in pairs.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

@@ -151,3 +151,25 @@ def test_render_into_device_tensor(cuda_device):
     out = torch.zeros((16, 16, 3), dtype=torch.float32, device=cuda_device)
     sc.render(cam, spp=4, max_depth=4, seed=1, out=out)
     np.testing.assert_allclose(out.cpu().numpy(), host, rtol=1e-5, atol=1e-6)
+
+
+def test_autotune_picks_a_timed_configuration_with_identical_image(cuda_device):
+    """The autotuner times kernel variants and queue capacities on a probe and returns
+    params that render the same image as the defaults."""
+    from mcrt_gb300 import GpuScene, autotune, render_batch, scenes
+    jobs = scenes.cfg2_jobs(n_scenes=3, seed=7, max_level=4)
+    gs = [GpuScene(d) for d, _, _ in jobs]
+    cams = [c for _, c, _ in jobs]
+    for c in cams:
+        c.width, c.height = 48, 40
+    params = [dict(p, spp=4) for _, _, p in jobs]
+    tuned, rep = autotune(gs, cams, params)
+    assert len(rep["candidates"]) >= 5
+    assert all(c["ms"] > 0 for c in rep["candidates"])
+    best = rep["candidates"][rep["chosen"]]
+    assert best["ms"] == min(c["ms"] for c in rep["candidates"])
+    assert all(t["variant"] == best["variant"] and t["path_chunk"] == best["path_chunk"] for t in tuned)
+    a, _ = render_batch(gs, cams, params)
+    b, _ = render_batch(gs, cams, tuned)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
