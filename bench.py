@@ -166,7 +166,7 @@ def bench_cfg2(args):
     """64 procedural scenes of uneven size: one batched wavefront (CUDA graph per wave)
     against the same renders issued scene by scene."""
     import torch
-    from mcrt_gb300 import GpuScene, render_batch, scenes
+    from mcrt_gb300 import GpuScene, autotune, render_batch, scenes
     jobs = scenes.cfg2_jobs(64)
     t0 = time.time()
     gs = [GpuScene(d) for d, _, _ in jobs]
@@ -174,6 +174,9 @@ def bench_cfg2(args):
     cams = [c for _, c, _ in jobs]
     params = [dict(p, use_graph=True, schedule=args.schedule_id) for _, _, p in jobs]
     outs = [torch.empty((c.height, c.width, 3), device="cuda") for c in cams]
+    t0 = time.time()
+    params, tune = autotune(gs, cams, params)  # queue capacity and kernel variant for the batch
+    tune_s = time.time() - t0
     render_batch(gs, cams, params, outs)  # warm-up
     for s, c, p, o in zip(gs, cams, jobs, outs):
         s.render(c, out=o, schedule=args.schedule_id, **p[2])
@@ -198,6 +201,8 @@ def bench_cfg2(args):
             "batched_mrays_s": round(stb["rays"] / tb / 1e6, 1), "sequential_mrays_s": round(seq_rays / ts / 1e6, 1),
             "batched_msamples_s": round(paths / tb / 1e6, 1), "speedup_batched_vs_sequential": round(ts / tb, 3),
             "sequential_waves_ms": round(tw * 1e3, 2), "speedup_batched_vs_sequential_waves": round(tw / tb, 3),
+            "autotune": {"seconds": round(tune_s, 2), "probe_paths": tune["probe_paths"],
+                         "chosen": tune["candidates"][tune["chosen"]], "candidates": len(tune["candidates"])},
             "schedule": args.schedule, "waves": stb["waves"], "scene_setup_s": round(setup_s, 1), "triangles": int(sum(d.num_triangles
                                                                                                for d, _, _ in jobs))}
     print(json.dumps(line), flush=True)
@@ -275,6 +280,7 @@ def main():
                     help="stream: slots refilled with new paths as paths end; waves: fixed waves")
     ap.add_argument("--path-chunk", type=int, default=0, help="path slots in flight (0: library default)")
     ap.add_argument("--variant", type=int, default=0, help="traversal kernel variant bits (0: default policy)")
+    ap.add_argument("--autotune", action="store_true", help="pick path_chunk / variant with mcrt_autotune first")
     args = ap.parse_args()
     args.schedule_id = 0 if args.schedule == "stream" else 1
     if args.impl == "reference":
@@ -317,6 +323,12 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
     kw = dict(spp=p["spp"], max_depth=p["max_depth"], rr_depth=p["rr_depth"], traverse=traverse,
               schedule=args.schedule_id, path_chunk=args.path_chunk, variant=args.variant)
+    tune = None
+    if args.autotune:
+        from mcrt_gb300 import autotune
+        (tuned,), tune = autotune([sc], [cam], [kw])
+        kw.update(path_chunk=tuned["path_chunk"], variant=tuned["variant"])
+        args.path_chunk, args.variant = tuned["path_chunk"], tuned["variant"]
 
     def barrier():
         if dist:
@@ -414,6 +426,7 @@ def main():
             "config": {"workload": text, "traversal": args.traverse, "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"replicas x{world}", "schedule": args.schedule,
                        "path_slots": args.path_chunk or "default", "variant": args.variant,
+                       "autotuned": tune is not None,
                        "waves_or_iterations_per_step": st_last["waves"],
                        "scene_setup_s": round(setup_s, 2), "scene_device_bytes": sc.info()["device_bytes"], "fast_nodes": sc.info()["fast_nodes"]},
             "msamples_per_s": round(msamples, 3),
