@@ -173,3 +173,18 @@ def test_autotune_picks_a_timed_configuration_with_identical_image(cuda_device):
     b, _ = render_batch(gs, cams, tuned)
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.parametrize("variant", [4 | 1 | 2 | 8, 4, 4 | 1, 4 | 2])
+def test_kernel_variants_render_identical_images(variant, cuda_device):
+    """Stack depth, register cap and work distribution change only how rays
+    are traced, never a path's result."""
+    from mcrt_gb300 import GpuScene, scenes
+    desc = scenes.cfg1_scene(level=5, env_size=(256, 128), patch_tris=64)
+    cam = scenes.cfg1_camera(48, 40)
+    sc = GpuScene(desc)
+    kw = dict(spp=4, max_depth=6, seed=3, path_chunk=1024)
+    a, sa = sc.render(cam, **kw)
+    b, sb = sc.render(cam, variant=variant, **kw)
+    np.testing.assert_array_equal(a, b)
+    assert sa["rays"] == sb["rays"]
