@@ -751,6 +751,24 @@ __device__ __forceinline__ int lower_bound_cdf(const float* cdf, int n, float r)
     return begin;
 }
 
+// lower_bound_cdf with the search started from a guide table (guide[g] = the lower bound of
+// g / G, G a power of two): the answer for r lies in [guide[g], guide[g + 1]] with
+// g = floor(r * G), so the result is the full search's, in a few steps
+__device__ __forceinline__ int lower_bound_guided(const float* cdf, const int* guide, int G, float r)
+{
+    const int g = clampi(static_cast<int>(r * static_cast<float>(G)), 0, G - 1);
+    int       begin = __ldg(guide + g), end = __ldg(guide + g + 1);
+    while (end > begin)
+    {
+        int mid = begin + (end - begin) / 2;
+        if (__ldg(cdf + mid) >= r)
+            end = mid;
+        else
+            begin = mid + 1;
+    }
+    return begin;
+}
+
 __device__ __forceinline__ float env_pdf_at(const SceneView& s, int ui, int vi)
 {
     float lum = __ldg(&s.env_rgb[ui + vi * s.env_w].w);
@@ -785,8 +803,9 @@ __device__ __forceinline__ void env_sample(const SceneView& s, float r1, float r
                                            float3& rad, float& pdf)
 {
     int   W = s.env_w, H = s.env_h;
-    int   ui0 = lower_bound_cdf(s.env_marginal, W, r1);
-    int   vi0 = lower_bound_cdf(s.env_cond + static_cast<size_t>(ui0) * H, H, r2);
+    int   ui0 = lower_bound_guided(s.env_marginal, s.env_guide_m, kEnvGuideM, r1);
+    int   vi0 = lower_bound_guided(s.env_cond + static_cast<size_t>(ui0) * H,
+                                   s.env_guide_c + static_cast<size_t>(ui0) * (kEnvGuideC + 1), kEnvGuideC, r2);
     float u = (static_cast<float>(ui0) + j1) / static_cast<float>(W);
     float v = (static_cast<float>(vi0) + j2) / static_cast<float>(H);
     int   ui = clampi(static_cast<int>(u * static_cast<float>(W)), 0, W - 1);

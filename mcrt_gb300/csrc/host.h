@@ -49,6 +49,8 @@ struct HostScene
     std::vector<float4>      env_rgb;
     std::vector<float>       env_marginal;
     std::vector<float>       env_cond;
+    std::vector<int32_t>     env_guide_m;  // kEnvGuideM + 1 entries
+    std::vector<int32_t>     env_guide_c;  // per column kEnvGuideC + 1 entries
     float                    env_norm = 0.f;
 };
 

@@ -1823,6 +1823,10 @@ int mcrt_scene_create(const mcrt_scene_desc* desc, mcrt_scene** out)
         up(hs.env_rgb, &er);
         up(hs.env_marginal, &em);
         up(hs.env_cond, &ec);
+        const int* egm;
+        const int* egc;
+        up(hs.env_guide_m, &egm);
+        up(hs.env_guide_c, &egc);
         if (rc != MCRT_OK)
         {
             std::string msg = g_err;
@@ -1842,6 +1846,8 @@ int mcrt_scene_create(const mcrt_scene_desc* desc, mcrt_scene** out)
         v.env_rgb = er;
         v.env_marginal = em;
         v.env_cond = ec;
+        v.env_guide_m = egm;
+        v.env_guide_c = egc;
         v.num_lights = static_cast<int>(hs.lights.size());
         v.light_area = hs.light_area;
         v.env_w = hs.env_w;

@@ -68,6 +68,10 @@ struct __align__(16) LightGPU
 };
 
 // Read-only view of one uploaded scene (device pointers).
+// guide-table resolution of the environment-map CDF searches (powers of two)
+constexpr int kEnvGuideM = 256;
+constexpr int kEnvGuideC = 64;
+
 struct SceneView
 {
     const FastNode*    fast_nodes;
@@ -82,6 +86,8 @@ struct SceneView
     const float4*      env_rgb;       // W*H texels, .w = un-warped luminance
     const float*       env_marginal;  // W column CDF
     const float*       env_cond;      // W*H: per column, H-entry CDF (column-major)
+    const int*         env_guide_m;   // kEnvGuideM + 1: lower bound of g / kEnvGuideM in env_marginal
+    const int*         env_guide_c;   // W*(kEnvGuideC + 1): the same per column of env_cond
     int                num_lights;
     float              light_area;
     int                env_w, env_h;

@@ -42,6 +42,21 @@ inline float  ibits(int32_t i)
 }
 
 // DiscreteSampler::update: pdf = data * (1 / sum), cdf = running float sum
+// first index i of cdf[0..n-1] with cdf[i] >= r, or n - 1 (the device search, same loop)
+int lower_bound_cdf_host(const float* cdf, int n, float r)
+{
+    int begin = 0, end = n - 1;
+    while (end > begin)
+    {
+        int mid = begin + (end - begin) / 2;
+        if (cdf[mid] >= r)
+            end = mid;
+        else
+            begin = mid + 1;
+    }
+    return begin;
+}
+
 void discrete(const std::vector<float>& data, std::vector<float>& pdf, std::vector<float>& cdf)
 {
     pdf = data;
@@ -202,6 +217,17 @@ std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs)
         }
         discrete(colsum, pdf, cdf);
         hs.env_marginal = cdf;
+        // guide tables: entry g = the lower bound of g / G, so a search for r starts in
+        // [guide[g], guide[g + 1]] with g = floor(r * G) (exact: G is a power of two)
+        auto guide = [](const float* c, int n, int G, int32_t* out) {
+            for (int g = 0; g <= G; ++g) out[g] = lower_bound_cdf_host(c, n, static_cast<float>(g) / G);
+        };
+        hs.env_guide_m.resize(kEnvGuideM + 1);
+        guide(hs.env_marginal.data(), N, kEnvGuideM, hs.env_guide_m.data());
+        hs.env_guide_c.resize(static_cast<size_t>(N) * (kEnvGuideC + 1));
+        for (int k = 0; k < N; ++k)
+            guide(&hs.env_cond[static_cast<size_t>(k) * M], M, kEnvGuideC,
+                  &hs.env_guide_c[static_cast<size_t>(k) * (kEnvGuideC + 1)]);
     }
     return std::string();
 }
