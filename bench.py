@@ -281,6 +281,7 @@ def main():
     ap.add_argument("--path-chunk", type=int, default=0, help="path slots in flight (0: library default)")
     ap.add_argument("--variant", type=int, default=0, help="traversal kernel variant bits (0: default policy)")
     ap.add_argument("--autotune", action="store_true", help="pick path_chunk / variant with mcrt_autotune first")
+    ap.add_argument("--leaf-size", type=int, default=4, help="BVH leaf size of the scene build (1..15)")
     args = ap.parse_args()
     args.schedule_id = 0 if args.schedule == "stream" else 1
     if args.impl == "reference":
@@ -316,7 +317,7 @@ def main():
         p["spp"] = args.spp
         text += f" [reduced: {args.spp} spp]"
     t0 = time.time()
-    sc = GpuScene(desc)
+    sc = GpuScene(desc, leaf_size=args.leaf_size)
     setup_s = time.time() - t0
     traverse = TRAVERSE_FAST if args.traverse == "fast" else TRAVERSE_REF
     out = torch.empty((cam.height, cam.width, 3), dtype=torch.float32, device=dev)
@@ -426,6 +427,7 @@ def main():
             "config": {"workload": text, "traversal": args.traverse, "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"replicas x{world}", "schedule": args.schedule,
                        "path_slots": args.path_chunk or "default", "variant": args.variant,
+                       "leaf_size": args.leaf_size,
                        "autotuned": tune is not None,
                        "waves_or_iterations_per_step": st_last["waves"],
                        "scene_setup_s": round(setup_s, 2), "scene_device_bytes": sc.info()["device_bytes"], "fast_nodes": sc.info()["fast_nodes"]},

@@ -4,7 +4,7 @@
 // The search is two-stage, so it costs about eight probe renders (each best of two):
 //   1. traversal kernel variants at the default queue capacity: 32-entry or 64-entry
 //      shared-memory stacks, 64-register cap or none, warp batch fetch or grid stride;
-//   2. queue capacities (2^19 .. 2^22 rays) with the best variant.
+//   2. queue capacities (2^21 .. 2^24 rays) with the best variant.
 // Every configuration renders the same image (the schedule never changes a path's
 // arithmetic), so only the time is compared.
 #include <cuda_runtime.h>
@@ -44,7 +44,7 @@ extern "C" int mcrt_autotune(int32_t num_jobs, mcrt_scene* const* scenes, const 
         }
         // probe: the same jobs with spp scaled so that the probe holds about four of the
         // largest candidate queues of paths (or the whole render if it is smaller)
-        constexpr int64_t kMaxCapacity = int64_t(1) << 22;
+        constexpr int64_t kMaxCapacity = int64_t(1) << 24;
         int64_t           total = 0;
         for (int j = 0; j < num_jobs; ++j)
             total += static_cast<int64_t>(cameras[j].width) * cameras[j].height * params[j].spp;
@@ -128,7 +128,7 @@ extern "C" int mcrt_autotune(int32_t num_jobs, mcrt_scene* const* scenes, const 
             }
         }
         int64_t best_chunk = 0;
-        for (int64_t chunk = int64_t(1) << 19; chunk <= kMaxCapacity; chunk <<= 1)
+        for (int64_t chunk = int64_t(1) << 21; chunk <= kMaxCapacity; chunk <<= 1)
         {
             if (chunk > 2 * probe_paths) break;
             float ms;

@@ -483,8 +483,11 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
 // Adjoint (ADJ): emission derivatives at emitter hits (the coefficient of E), and at a
 // parameterised Lambert vertex k the - dL/dI * L_before(k) / albedo_k half of the albedo
 // derivative; the vertex's material id goes to the path's log for the other half.
+// Registers capped at 64 (8 blocks per SM; measured faster than the uncapped 80).  One
+// build only: builds under different register budgets contract multiply-adds
+// differently, and every configuration must render the same image.
 template <bool ADJ>
-__global__ void __launch_bounds__(128) k_shade(WaveArgs a, int p)
+__global__ void __launch_bounds__(128, 8) k_shade(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];
     const Grads G = grads_begin<ADJ>(a, sgrad);
@@ -1602,7 +1605,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     const bool stages = (p0.profile & MCRT_PROFILE_STAGES) != 0;
     const bool graph = p0.use_graph && !stages;
     // variant 0: the default policy (32-entry stacks when the tree is shallow enough,
-    // registers capped for 8 blocks per SM); MCRT_VARIANT_EXPLICIT: the given bits
+    // traversal registers capped for 8 blocks per SM); MCRT_VARIANT_EXPLICIT: the given bits
     const int   vb = (p0.variant & MCRT_VARIANT_EXPLICIT) ? p0.variant : (MCRT_VARIANT_STACK32 | MCRT_VARIANT_REGCAP);
     const bool  stack32 = (vb & MCRT_VARIANT_STACK32) && bvh_depth + 2 < 32;
     const bool  regcap = (vb & MCRT_VARIANT_REGCAP) != 0;
