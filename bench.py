@@ -102,6 +102,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# DRAM bytes per average launch of the traversal kernels on the default cfg1 frame
+# (ncu dram__bytes_read.sum + dram__bytes_write.sum over every launch of three frames,
+# warm caches; profiles/cfg1_dram_traffic.md).  Valid only for that exact configuration.
+CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 437.5e6, "k_extend": 343.1e6}
+
+
 def measured_peak_hbm():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -392,6 +398,10 @@ def main():
     achieved = per_launch_bytes / (avg_launch_ms / 1e3) / 1e9 if avg_launch_ms > 0 else 0.0
     peak, peak_kind = measured_peak_hbm()
     other = [k for k in kernels if k != dom][0]
+    default_cfg1 = (args.workload == "cfg1" and not args.res and not args.spp and not args.path_chunk
+                    and not args.variant and args.traverse == "fast" and args.leaf_size == 4
+                    and args.schedule == "stream" and not args.autotune)
+    traffic = CFG1_DRAM_BYTES_PER_LAUNCH.get(dom.split()[0]) if default_cfg1 else None
     ob, oms = kernels[other][0], kernels[other][1]
     other_achieved = (ob / launches_per_render) / (oms / max(extend_launches, 1) / 1e3) / 1e9 if oms > 0 else 0.0
 
@@ -434,7 +444,10 @@ def main():
             "msamples_per_s": round(msamples, 3),
             "rays_per_path": round(rays / max(paths, 1), 3),
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
-                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": None if traffic is None else int(traffic),
+                         "traffic_unit": "bytes per launch (ncu DRAM read + write, warm caches)",
+                         "algorithmic_bytes_per_launch": int(per_launch_bytes),
                          "peak_source": peak_kind,
                          "bytes_per_ray": round(bytes_per_render / max(kern_rays, 1), 1),
                          "nodes_per_ray": round(kern_nodes / max(kern_rays, 1), 2),
