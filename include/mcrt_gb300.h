@@ -14,6 +14,8 @@
  *   SceneBVH::occluded            src/core/scenebvh.h:18, scenebvh.cpp:379-396 -> mcrt_trace_any
  *   SceneBVH::~SceneBVH           src/core/scenebvh.cpp:398-402                -> mcrt_scene_destroy
  *   rayTrace + DemoSimple::run    src/examples/pt/demo_pt.cpp:512-720        -> mcrt_render
+ *   FrameBuffer::dumpHDR/dumpPPM  src/core/film.cpp:9-108                    -> mcrt_film_encode
+ *   FrameBuffer::tonemap*         src/core/film.cpp:110-203                  -> mcrt_film_tonemap
  *   (no reference counterpart: path-replay adjoint, batched launch, tuning)   -> mcrt_render_adjoint,
  *                                                                                mcrt_render_adjoint_batch,
  *                                                                                mcrt_render_batch,
@@ -231,6 +233,23 @@ int mcrt_render_adjoint_batch(int32_t num_jobs, mcrt_scene* const* scenes, const
  * stage launch.  rgb_out[j] receives job j's image. */
 int mcrt_render_batch(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cameras,
                       const mcrt_render_params* params, float* const* rgb_out, mcrt_render_stats* stats,
+                      void* stream);
+
+/* Film outputs (FrameBuffer, src/core/film.cpp) on an image in mcrt_render's layout
+ * ([height][width][3] floats, row 0 the bottom row); ptr_mode says where rgb / out live.
+ *   mcrt_film_encode: the bytes of FrameBuffer::dumpHDR (MCRT_FILM_HDR, film.cpp:35-108:
+ *     Radiance header + RLE scanlines of literal runs) or dumpPPM (MCRT_FILM_PPM,
+ *     film.cpp:9-33), byte for byte.  out = NULL: only *size is set (the file size).
+ *   mcrt_film_tonemap: tonemapGamma(gamma) (MCRT_TONEMAP_GAMMA, film.cpp:196-203; the
+ *     per-pixel powf is CUDA's, within its ulp bound of the C library's) or
+ *     tonemapReinhard() (MCRT_TONEMAP_REINHARD, film.cpp:110-194, bit for bit), in place. */
+#define MCRT_FILM_HDR 0
+#define MCRT_FILM_PPM 1
+#define MCRT_TONEMAP_GAMMA 0
+#define MCRT_TONEMAP_REINHARD 1
+int mcrt_film_encode(const float* rgb, int32_t width, int32_t height, int32_t format, uint8_t* out,
+                     int64_t capacity, int64_t* size, int32_t ptr_mode, void* stream);
+int mcrt_film_tonemap(float* rgb, int32_t width, int32_t height, int32_t op, float gamma, int32_t ptr_mode,
                       void* stream);
 
 /* Autotuner (no reference counterpart).  Renders a reduced-spp probe of the jobs (the

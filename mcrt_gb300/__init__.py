@@ -8,11 +8,12 @@ Public surface:
   render_adjoint_batch                 the adjoint of render_batch in one launch
   autotune                             launch configuration (queue capacity, kernel variant)
                                        timed on a reduced-spp probe of the jobs
+  film                                 FrameBuffer's .hdr / .ppm writers and tone mappers on the GPU
   build()                              compile the in-tree native library
 The native library (mcrt_gb300/_lib/libmcrt_gb300.so, C ABI in include/mcrt_gb300.h)
 is required: there is no CPU fallback.
 """
-from . import scenes
+from . import film, scenes
 from ._native import (PTR_DEVICE, PTR_HOST, TRAVERSE_FAST, TRAVERSE_REF, McrtError, load)
 from .native_build import build
 from .scene import (DIFF, GGX, GLSY, LGHT, REFR, SPEC, CameraDesc, GpuScene, Material, SceneDesc, autotune,
@@ -20,6 +21,6 @@ from .scene import (DIFF, GGX, GLSY, LGHT, REFR, SPEC, CameraDesc, GpuScene, Mat
 
 __all__ = ["SceneDesc", "Material", "CameraDesc", "GpuScene", "render_batch", "render_adjoint_batch", "autotune",
            "build", "load",
-           "scenes",
+           "scenes", "film",
            "McrtError", "TRAVERSE_FAST", "TRAVERSE_REF", "PTR_HOST", "PTR_DEVICE", "make_params",
            "LGHT", "DIFF", "SPEC", "REFR", "GLSY", "GGX"]

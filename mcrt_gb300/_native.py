@@ -33,6 +33,10 @@ VARIANT_STACK32 = 1
 VARIANT_REGCAP = 2
 VARIANT_EXPLICIT = 4
 VARIANT_GRIDSTRIDE = 8
+FILM_HDR = 0
+FILM_PPM = 1
+TONEMAP_GAMMA = 0
+TONEMAP_REINHARD = 1
 SCHEDULE_STREAM = 0
 SCHEDULE_WAVES = 1
 BUILD_SAH = 0
@@ -113,6 +117,9 @@ EXPORTS = {
     "mcrt_render_batch": (c_int32, [c_int32, ctypes.POINTER(c_void_p), ctypes.POINTER(Camera),
                                     ctypes.POINTER(RenderParams), ctypes.POINTER(c_void_p),
                                     ctypes.POINTER(RenderStats), c_void_p]),
+    "mcrt_film_encode": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int64, ctypes.POINTER(c_int64),
+                                   c_int32, c_void_p]),
+    "mcrt_film_tonemap": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_float, c_int32, c_void_p]),
     "mcrt_autotune": (c_int32, [c_int32, ctypes.POINTER(c_void_p), ctypes.POINTER(Camera),
                                 ctypes.POINTER(RenderParams), ctypes.POINTER(RenderParams),
                                 ctypes.POINTER(TuneReport), c_void_p]),

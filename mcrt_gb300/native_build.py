@@ -20,7 +20,7 @@ LIB_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIB_DIR, "libmcrt_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["kernels.cu", "noalloc.cu"]
+CU_SOURCES = ["kernels.cu", "noalloc.cu", "film.cu"]
 CPP_SOURCES = ["bvh_build.cpp", "flatten.cpp", "scene_prep.cpp", "autotune.cpp"]
 HEADERS = ["layout.h", "host.h", "device.cuh", "estimator.cuh", "wavefront.h"]
 
@@ -55,7 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         o = os.path.join(LIB_DIR, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            jobs.append([nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                          "-Xptxas", "-warn-spills", "-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)

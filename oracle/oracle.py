@@ -84,6 +84,11 @@ def load_restatement():
         lib.orc_envmap_radiance.argtypes = [P, P, P]
         lib.orc_envmap_sample_texel.argtypes = [P, F, F, P, P]
         lib.orc_pcg32.argtypes = [ctypes.c_ulonglong, ctypes.c_uint, ctypes.c_uint, I, P]
+        lib.orc_film_hdr.restype = LL
+        lib.orc_film_hdr.argtypes = [I, I, P, P, LL]
+        lib.orc_film_ppm.restype = LL
+        lib.orc_film_ppm.argtypes = [I, I, P, P, LL]
+        lib.orc_film_tonemap.argtypes = [I, I, P, I, F]
         _orc = lib
     return _orc
 
@@ -135,12 +140,35 @@ def load_reference():
         lib.ref_cornell_paths.argtypes = [I, I, I, P, P]
         lib.ref_render_cornell.restype = I
         lib.ref_render_cornell.argtypes = [I, I, I, I, I, I, P, P, P, P]
+        lib.ref_film_dump.argtypes = [I, I, P, ctypes.c_char_p, I]
+        lib.ref_film_tonemap.argtypes = [I, I, P, I, F]
         _ref = lib
     return _ref
 
 
 def ptr(a: np.ndarray | None):
     return None if a is None else a.ctypes.data
+
+
+def film_encode(rgb: np.ndarray, hdr: bool) -> bytes:
+    """The oracle's FrameBuffer::dumpHDR / dumpPPM bytes of an [h][w][3] image (row 0 the
+    bottom row)."""
+    lib = load_restatement()
+    img = np.ascontiguousarray(rgb, np.float32)
+    h, w = img.shape[:2]
+    fn = lib.orc_film_hdr if hdr else lib.orc_film_ppm
+    n = fn(w, h, ptr(img), None, 0)
+    out = np.zeros(n, np.uint8)
+    fn(w, h, ptr(img), ptr(out), n)
+    return out.tobytes()
+
+
+def film_tonemap(rgb: np.ndarray, reinhard: bool, gamma: float = 2.2) -> np.ndarray:
+    """The oracle's FrameBuffer::tonemapReinhard / tonemapGamma(gamma) of an image."""
+    lib = load_restatement()
+    img = np.array(rgb, np.float32, copy=True, order="C")
+    lib.orc_film_tonemap(img.shape[1], img.shape[0], ptr(img), 1 if reinhard else 0, gamma)
+    return img
 
 
 class OracleScene:

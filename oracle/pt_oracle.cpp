@@ -49,6 +49,7 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -1724,6 +1725,126 @@ void orc_pcg32(unsigned long long seed, unsigned pixel, unsigned sample, int n, 
     Pcg32 r;
     r.seed(seed, pixel, sample);
     for (int i = 0; i < n; ++i) out[i] = r.uniform();
+}
+
+// ---------------------------------------------------------------------------
+// Film outputs, restated from film.cpp.  Images are [h][w][3] floats with row 0 the
+// bottom row (FrameBuffer's layout); both writers emit rows top to bottom.
+// ---------------------------------------------------------------------------
+
+// FrameBuffer::dumpHDR (film.cpp:35-108): Radiance header, then per row the new-style
+// RLE scanline marker and four channel blocks of literal runs (<= 127 bytes, no repeats).
+// Returns the file size; writes it to out when capacity allows.
+long long orc_film_hdr(int w, int h, const float* rgb, unsigned char* out, long long capacity)
+{
+    std::string head = "#?RADIANCE\n# Made with custom writer\nFORMAT=32-bit_rle_rgbe\nEXPOSURE=1.0\n\n-Y " +
+                       std::to_string(h) + " +X " + std::to_string(w) + "\n";
+    std::vector<unsigned char> f(head.begin(), head.end());
+    std::vector<unsigned char> line(4 * static_cast<size_t>(w));
+    for (int j = h - 1; j >= 0; --j)
+    {
+        for (int i = 0; i < w; ++i)
+        {
+            const float* c = rgb + 3 * (static_cast<size_t>(j) * w + i);
+            // toRGBE (film.cpp:49-64): d = m 2^e, scale = m * 256 / d = 2^(8 - e)
+            float d = c[0] > c[1] ? c[0] : c[1];
+            d = d > c[2] ? d : c[2];
+            unsigned char* q = &line[4 * static_cast<size_t>(i)];
+            if (d <= 1e-32)
+            {
+                q[0] = q[1] = q[2] = q[3] = 0;
+                continue;
+            }
+            int   e;
+            float m = static_cast<float>(std::frexp(static_cast<double>(d), &e));
+            float s = m * 256.0f / d;
+            q[0] = static_cast<unsigned char>(c[0] * s);
+            q[1] = static_cast<unsigned char>(c[1] * s);
+            q[2] = static_cast<unsigned char>(c[2] * s);
+            q[3] = static_cast<unsigned char>(e + 128);
+        }
+        f.push_back(2);
+        f.push_back(2);
+        f.push_back(static_cast<unsigned char>((w >> 8) & 0xFF));
+        f.push_back(static_cast<unsigned char>(w & 0xFF));
+        for (int k = 0; k < 4; ++k)
+            for (int cursor = 0; cursor < w;)
+            {
+                const int run = std::min(127, w - cursor);
+                f.push_back(static_cast<unsigned char>(run));
+                for (int i = cursor; i < cursor + run; ++i) f.push_back(line[4 * static_cast<size_t>(i) + k]);
+                cursor += run;
+            }
+    }
+    if (out && capacity >= static_cast<long long>(f.size())) std::memcpy(out, f.data(), f.size());
+    return static_cast<long long>(f.size());
+}
+
+// FrameBuffer::dumpPPM (film.cpp:9-33): "P6 w h 255", bytes (unsigned char)(min(1, v) * 255)
+long long orc_film_ppm(int w, int h, const float* rgb, unsigned char* out, long long capacity)
+{
+    std::string head = "P6\n" + std::to_string(w) + " " + std::to_string(h) + "\n255\n";
+    std::vector<unsigned char> f(head.begin(), head.end());
+    for (int j = h - 1; j >= 0; --j)
+        for (int i = 0; i < w; ++i)
+            for (int k = 0; k < 3; ++k)
+            {
+                float v = rgb[3 * (static_cast<size_t>(j) * w + i) + k];
+                f.push_back(static_cast<unsigned char>((1.0f < v ? 1.0f : v) * 255));
+            }
+    if (out && capacity >= static_cast<long long>(f.size())) std::memcpy(out, f.data(), f.size());
+    return static_cast<long long>(f.size());
+}
+
+// FrameBuffer::tonemapGamma (mode 0, film.cpp:196-203) and tonemapReinhard (mode 1,
+// film.cpp:110-194; its contrast is fixed at 0.77 and light adaptation at 0, so every
+// pixel maps x -> x / (x + (c * mean_x + (1 - c) * mean_lum)^0.77), c = 0.5, with the
+// means accumulated in float in pixel order), in place
+void orc_film_tonemap(int w, int h, float* rgb, int mode, float gamma)
+{
+    const size_t n = static_cast<size_t>(w) * h;
+    if (mode == 0)
+    {
+        const float inv = 1.0f / gamma;
+        for (size_t k = 0; k < 3 * n; ++k)
+        {
+            float x = rgb[k];
+            x = x < 0.0f ? 0.0f : x > 1.0f ? 1.0f : x;
+            rgb[k] = powf(x, inv);
+        }
+        return;
+    }
+    std::vector<float> lum(n);
+    float              l_mean = 0, r_mean = 0, g_mean = 0, b_mean = 0;
+    for (size_t p = 0; p < n; ++p)
+    {
+        const float* c = rgb + 3 * p;
+        // luminance (numeric.cpp:62-66) in double
+        lum[p] = static_cast<float>(0.299 * c[0] + 0.587 * c[1] + 0.114 * c[2]);
+        if (lum[p] < 1e-7f) lum[p] = 1e-7f;
+    }
+    for (size_t p = 0; p < n; ++p)
+    {
+        l_mean += lum[p];
+        r_mean += rgb[3 * p];
+        g_mean += rgb[3 * p + 1];
+        b_mean += rgb[3 * p + 2];
+    }
+    l_mean /= n;
+    r_mean /= n;
+    g_mean /= n;
+    b_mean /= n;
+    const float c = 0.5f, m = 0.77f, f = expf(-0.0f);
+    const float kr = powf(f * (c * r_mean + (1.0f - c) * l_mean), m);
+    const float kg = powf(f * (c * g_mean + (1.0f - c) * l_mean), m);
+    const float kb = powf(f * (c * b_mean + (1.0f - c) * l_mean), m);
+    for (size_t p = 0; p < n; ++p)
+    {
+        float* x = rgb + 3 * p;
+        x[0] = x[0] / (x[0] + kr);
+        x[1] = x[1] / (x[1] + kg);
+        x[2] = x[2] / (x[2] + kb);
+    }
 }
 
 }  // extern "C"

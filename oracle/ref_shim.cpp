@@ -498,3 +498,51 @@ extern "C" int ref_render_cornell(int width, int height, int spp, int nthreads, 
     if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
     return 0;
 }
+
+// --- film outputs (film.cpp): FrameBuffer filled through accumulatePixel (0 + x = x) -----
+static void fill_fb(FrameBuffer& fb, int w, int h, const float* rgb)
+{
+    fb.resize(w, h);
+    for (int j = 0; j < h; ++j)
+        for (int i = 0; i < w; ++i)
+        {
+            const float* c = rgb + 3 * (static_cast<size_t>(j) * w + i);
+            fb.accumulatePixel(i, j, vec3(c[0], c[1], c[2]));
+        }
+}
+
+static void read_fb(const FrameBuffer& fb, int w, int h, float* rgb)
+{
+    for (int j = 0; j < h; ++j)
+        for (int i = 0; i < w; ++i)
+        {
+            vec3   c = fb.pixel(i, j);
+            float* o = rgb + 3 * (static_cast<size_t>(j) * w + i);
+            o[0] = c.x;
+            o[1] = c.y;
+            o[2] = c.z;
+        }
+}
+
+// FrameBuffer::dumpHDR / dumpPPM to `path`
+extern "C" void ref_film_dump(int w, int h, const float* rgb, const char* path, int hdr)
+{
+    FrameBuffer fb;
+    fill_fb(fb, w, h, rgb);
+    if (hdr)
+        fb.dumpHDR(path);
+    else
+        fb.dumpPPM(path);
+}
+
+// FrameBuffer::tonemapGamma (mode 0, with `gamma`) or tonemapReinhard (mode 1), in place
+extern "C" void ref_film_tonemap(int w, int h, float* rgb, int mode, float gamma)
+{
+    FrameBuffer fb;
+    fill_fb(fb, w, h, rgb);
+    if (mode == 0)
+        fb.tonemapGamma(gamma);
+    else
+        fb.tonemapReinhard();
+    read_fb(fb, w, h, rgb);
+}

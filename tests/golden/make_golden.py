@@ -289,10 +289,49 @@ def cornell_paths_fixture(ref, res=16, spp=8):
     print(f"cornell paths: {res}x{res}x{spp} samples, {draws[-1]} draws")
 
 
+def film_images(rng):
+    """Test images for the film writers: radiance over many octaves, exact zeros, values
+    below the RGBE cut-off, exact powers of two, values above 1 for the PPM clamp; one
+    image wider than 255 pixels (two-byte scanline width, several 127-byte runs)."""
+    imgs = []
+    for (h, w) in ((23, 37), (5, 300), (1, 1), (3, 127), (2, 128)):
+        a = np.exp(rng.uniform(-9.0, 7.0, (h, w, 3))).astype(np.float32)
+        a[rng.uniform(size=(h, w)) < 0.08] = 0.0
+        a[rng.uniform(size=(h, w)) < 0.04] = 1e-33
+        a[rng.uniform(size=(h, w, 3)) < 0.05] = 2.0 ** rng.integers(-6, 7, 1)[0]
+        imgs.append(a)
+    return imgs
+
+
+def film_fixture(ref):
+    """FrameBuffer::dumpHDR / dumpPPM bytes and tonemapGamma / tonemapReinhard outputs of
+    the reference (film.cpp) for seeded images."""
+    import tempfile
+    rng = np.random.default_rng(33)
+    out = {}
+    for k, img in enumerate(film_images(rng)):
+        h, w = img.shape[:2]
+        out[f"img{k}"] = img
+        with tempfile.TemporaryDirectory() as d:
+            for hdr, ext in ((1, "hdr"), (0, "ppm")):
+                path = os.path.join(d, f"f.{ext}")
+                ref.ref_film_dump(w, h, ptr(img), path.encode(), hdr)
+                out[f"{ext}{k}"] = np.frombuffer(open(path, "rb").read(), np.uint8)
+        for mode, name in ((0, "gamma"), (1, "reinhard")):
+            t = np.array(img, np.float32, copy=True)
+            ref.ref_film_tonemap(w, h, ptr(t), mode, 2.2)
+            out[f"{name}{k}"] = t
+    np.savez_compressed(os.path.join(OUT, "ref_film.npz"), **out)
+
+
 def main():
     ref = O.load_reference()
     if ref is None:
         raise SystemExit("reference sources not available: cannot regenerate fixtures")
+    if "--only-film" in sys.argv:
+        film_fixture(ref)
+        return
+    film_fixture(ref)
     cornell_paths_fixture(ref)  # first: the global random stream starts at its seed here
     rng = np.random.default_rng(20261203)
     # the reference's own Cornell box (demo_pt.cpp:83-414)

@@ -1,6 +1,7 @@
 """The oracle (CPU restatement) pinned against the reference's own outputs (golden
 fixtures generated from the compiled reference), and against the reference library
 directly where it is available."""
+import os
 import numpy as np
 import pytest
 
@@ -226,3 +227,19 @@ def test_oracle_against_reference_library_directly():
                                     float(r2), b_wo.ctypes.data, b_w.ctypes.data, ctypes.byref(p2))
             assert np.array_equal(a_w, b_w)
             np.testing.assert_allclose(a_wo, b_wo, rtol=1e-6, atol=1e-7)
+
+
+def test_film_writers_and_tonemaps_match_reference():
+    """The oracle's restatement of film.cpp against the reference's own FrameBuffer:
+    dumpHDR / dumpPPM byte for byte, tonemapGamma / tonemapReinhard bit for bit."""
+    from oracle import oracle as O
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_film.npz"))
+    k = 0
+    while f"img{k}" in g:
+        img = g[f"img{k}"]
+        assert O.film_encode(img, True) == g[f"hdr{k}"].tobytes(), f"hdr {k}"
+        assert O.film_encode(img, False) == g[f"ppm{k}"].tobytes(), f"ppm {k}"
+        np.testing.assert_array_equal(O.film_tonemap(img, False, 2.2), g[f"gamma{k}"])
+        np.testing.assert_array_equal(O.film_tonemap(img, True), g[f"reinhard{k}"])
+        k += 1
+    assert k == 5
