@@ -177,6 +177,18 @@ def bench_cfg2(args):
     t0 = time.time()
     gs = [GpuScene(d) for d, _, _ in jobs]
     setup_s = time.time() - t0
+    # the same 64 scenes from scene cache files (mcrt_scene_save / mcrt_scene_load)
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        paths = [os.path.join(tmp, f"s{k}.mcrt") for k in range(len(gs))]
+        for g, pth in zip(gs, paths):
+            g.save(pth)
+        t0 = time.time()
+        loaded = [GpuScene.load(pth, d) for pth, (d, _, _) in zip(paths, jobs)]
+        load_s = time.time() - t0
+        cache_mb = sum(os.path.getsize(pth) for pth in paths) / 1e6
+        for g in loaded:
+            g.close()
     cams = [c for _, c, _ in jobs]
     params = [dict(p, use_graph=True, schedule=args.schedule_id) for _, _, p in jobs]
     outs = [torch.empty((c.height, c.width, 3), device="cuda") for c in cams]
@@ -209,7 +221,9 @@ def bench_cfg2(args):
             "sequential_waves_ms": round(tw * 1e3, 2), "speedup_batched_vs_sequential_waves": round(tw / tb, 3),
             "autotune": {"seconds": round(tune_s, 2), "probe_paths": tune["probe_paths"],
                          "chosen": tune["candidates"][tune["chosen"]], "candidates": len(tune["candidates"])},
-            "schedule": args.schedule, "waves": stb["waves"], "scene_setup_s": round(setup_s, 1), "triangles": int(sum(d.num_triangles
+            "schedule": args.schedule, "waves": stb["waves"], "scene_setup_s": round(setup_s, 1),
+            "scene_cache_load_s": round(load_s, 2), "scene_cache_mb": round(cache_mb, 1),
+            "triangles": int(sum(d.num_triangles
                                                                                                for d, _, _ in jobs))}
     print(json.dumps(line), flush=True)
 

@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/mcrt_gb300.h"
 #include "layout.h"
 
 namespace mcrt {
@@ -53,5 +54,13 @@ struct HostScene
     std::vector<int32_t>     env_guide_c;  // per column kEnvGuideC + 1 entries
     float                    env_norm = 0.f;
 };
+
+// the library's device scene from / to its prepared host arrays (scene cache files)
+int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, mcrt_scene** out);
+int scene_to_host(const mcrt_scene* s, HostScene& hs, int64_t& num_tris, uint64_t& desc_hash);
+// FNV-1a 64 of everything a scene is built from, and of the cache format version
+uint64_t scene_desc_hash(const mcrt_scene_desc& d);
+// prepared host arrays from a scene description (builder, flattener, sampling tables)
+std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs);
 
 }  // namespace mcrt

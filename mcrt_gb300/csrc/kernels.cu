@@ -33,7 +33,6 @@
 #include "wavefront.h"
 
 namespace mcrt {
-std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs);
 
 
 // ---------------------------------------------------------------------------
@@ -976,6 +975,8 @@ struct mcrt_scene
     int                device = 0;
     int                num_materials = 0;
     MaterialGPU*       d_materials = nullptr;
+    std::vector<int64_t> array_bytes;  // bytes of each uploaded array, in upload order
+    uint64_t             desc_hash = 0;  // of the description the scene was built from
     int*               d_err = nullptr;
     Workspace          ws;
     std::mutex         mu;
@@ -1758,6 +1759,123 @@ void enqueue_wave_plain(const WaveArgs& a, int max_depth, const LaunchShape& ls,
 
 CameraGPU make_camera(const mcrt_camera& c) { return make_camera_impl(c); }
 
+// uploads a prepared scene; the arrays are kept in upload order with their byte counts so
+// the scene can be written to a cache file (scene_to_host)
+int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, mcrt_scene** out)
+{
+    mcrt_scene* s = new mcrt_scene();
+    CK(cudaGetDevice(&s->device));
+    int  rc = MCRT_OK;
+    auto up = [&](auto& vec, auto** dst) {
+        if (rc == MCRT_OK) rc = upload(s, vec, dst);
+        s->array_bytes.push_back(static_cast<int64_t>(vec.size() * sizeof(vec[0])));
+    };
+    const FastNode*    fn;
+    const float4*      ft;
+    const RefNode*     rn;
+    const RefPrim*     rp;
+    const float4*      pv;
+    const float4*      ps;
+    const int*         lo;
+    const LightGPU*    li;
+    const MaterialGPU* mt;
+    const float4*      er;
+    const float*       em;
+    const float*       ec;
+    const int*         egm;
+    const int*         egc;
+    up(hs.bvh.fast_nodes, &fn);
+    up(hs.bvh.fast_tris, &ft);
+    up(hs.bvh.ref_nodes, &rn);
+    up(hs.bvh.ref_prims, &rp);
+    up(hs.prim_verts, &pv);
+    up(hs.prim_shade, &ps);
+    up(hs.light_of, &lo);
+    up(hs.lights, &li);
+    up(hs.materials, &mt);
+    up(hs.env_rgb, &er);
+    up(hs.env_marginal, &em);
+    up(hs.env_cond, &ec);
+    up(hs.env_guide_m, &egm);
+    up(hs.env_guide_c, &egc);
+    if (rc != MCRT_OK)
+    {
+        std::string msg = g_err;
+        mcrt_scene_destroy(s);
+        return fail(rc, msg);
+    }
+    SceneView& v = s->view;
+    v.fast_nodes = fn;
+    v.fast_tris = ft;
+    v.ref_nodes = rn;
+    v.ref_prims = rp;
+    v.prim_verts = pv;
+    v.prim_shade = ps;
+    v.light_of = lo;
+    v.lights = li;
+    v.materials = mt;
+    v.env_rgb = er;
+    v.env_marginal = em;
+    v.env_cond = ec;
+    v.env_guide_m = egm;
+    v.env_guide_c = egc;
+    v.num_lights = static_cast<int>(hs.lights.size());
+    v.light_area = hs.light_area;
+    v.env_w = hs.env_w;
+    v.env_h = hs.env_h;
+    v.env_norm = hs.env_norm;
+    v.num_prims = static_cast<int>(num_tris);
+    s->d_materials = const_cast<MaterialGPU*>(mt);
+    s->num_materials = static_cast<int>(hs.materials.size());
+    s->fast_nodes = static_cast<int64_t>(hs.bvh.fast_nodes.size());
+    s->ref_nodes = static_cast<int64_t>(hs.bvh.ref_nodes.size());
+    s->refs = static_cast<int64_t>(hs.bvh.ref_prims.size());
+    s->bvh_depth = hs.bvh.max_depth;
+    s->desc_hash = desc_hash;
+    *out = s;
+    return MCRT_OK;
+}
+
+// downloads a scene's prepared arrays (the inverse of scene_from_host)
+int scene_to_host(const mcrt_scene* s, HostScene& hs, int64_t& num_tris, uint64_t& desc_hash)
+{
+    if (s->array_bytes.size() != 14) return fail(MCRT_ERR_INTERNAL, "scene arrays not recorded");
+    CK(cudaSetDevice(s->device));
+    const SceneView& v = s->view;
+    int              k = 0, rc = MCRT_OK;
+    auto             down = [&](auto& vec, const void* src) {
+        const int64_t bytes = s->array_bytes[k++];
+        vec.resize(static_cast<size_t>(bytes) / sizeof(vec[0]));
+        if (rc == MCRT_OK && bytes > 0)
+        {
+            cudaError_t e = cudaMemcpy(vec.data(), src, static_cast<size_t>(bytes), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) rc = fail(MCRT_ERR_CUDA, std::string("scene download: ") + cudaGetErrorString(e));
+        }
+    };
+    down(hs.bvh.fast_nodes, v.fast_nodes);
+    down(hs.bvh.fast_tris, v.fast_tris);
+    down(hs.bvh.ref_nodes, v.ref_nodes);
+    down(hs.bvh.ref_prims, v.ref_prims);
+    down(hs.prim_verts, v.prim_verts);
+    down(hs.prim_shade, v.prim_shade);
+    down(hs.light_of, v.light_of);
+    down(hs.lights, v.lights);
+    down(hs.materials, v.materials);
+    down(hs.env_rgb, v.env_rgb);
+    down(hs.env_marginal, v.env_marginal);
+    down(hs.env_cond, v.env_cond);
+    down(hs.env_guide_m, v.env_guide_m);
+    down(hs.env_guide_c, v.env_guide_c);
+    hs.light_area = v.light_area;
+    hs.env_w = v.env_w;
+    hs.env_h = v.env_h;
+    hs.env_norm = v.env_norm;
+    hs.bvh.max_depth = s->bvh_depth;
+    num_tris = v.num_prims;
+    desc_hash = s->desc_hash;
+    return rc;
+}
+
 int validate_job(const mcrt_scene* s, const mcrt_camera* c, const mcrt_render_params* p)
 {
     return validate_job_impl(s, c, p);
@@ -1796,75 +1914,7 @@ int mcrt_scene_create(const mcrt_scene_desc* desc, mcrt_scene** out)
         HostScene   hs;
         std::string err = prepare_scene(*desc, hs);
         if (!err.empty()) return fail(MCRT_ERR_INVALID_ARGUMENT, err);
-        mcrt_scene* s = new mcrt_scene();
-        CK(cudaGetDevice(&s->device));
-        int rc = MCRT_OK;
-        auto up = [&](auto& vec, auto** dst) {
-            if (rc == MCRT_OK) rc = upload(s, vec, dst);
-        };
-        const FastNode*    fn;
-        const float4*      ft;
-        const RefNode*     rn;
-        const RefPrim*     rp;
-        const float4*      pv;
-        const float4*      ps;
-        const int*         lo;
-        const LightGPU*    li;
-        const MaterialGPU* mt;
-        const float4*      er;
-        const float*       em;
-        const float*       ec;
-        up(hs.bvh.fast_nodes, &fn);
-        up(hs.bvh.fast_tris, &ft);
-        up(hs.bvh.ref_nodes, &rn);
-        up(hs.bvh.ref_prims, &rp);
-        up(hs.prim_verts, &pv);
-        up(hs.prim_shade, &ps);
-        up(hs.light_of, &lo);
-        up(hs.lights, &li);
-        up(hs.materials, &mt);
-        up(hs.env_rgb, &er);
-        up(hs.env_marginal, &em);
-        up(hs.env_cond, &ec);
-        const int* egm;
-        const int* egc;
-        up(hs.env_guide_m, &egm);
-        up(hs.env_guide_c, &egc);
-        if (rc != MCRT_OK)
-        {
-            std::string msg = g_err;
-            mcrt_scene_destroy(s);
-            return fail(rc, msg);
-        }
-        SceneView& v = s->view;
-        v.fast_nodes = fn;
-        v.fast_tris = ft;
-        v.ref_nodes = rn;
-        v.ref_prims = rp;
-        v.prim_verts = pv;
-        v.prim_shade = ps;
-        v.light_of = lo;
-        v.lights = li;
-        v.materials = mt;
-        v.env_rgb = er;
-        v.env_marginal = em;
-        v.env_cond = ec;
-        v.env_guide_m = egm;
-        v.env_guide_c = egc;
-        v.num_lights = static_cast<int>(hs.lights.size());
-        v.light_area = hs.light_area;
-        v.env_w = hs.env_w;
-        v.env_h = hs.env_h;
-        v.env_norm = hs.env_norm;
-        v.num_prims = static_cast<int>(desc->num_triangles);
-        s->d_materials = const_cast<MaterialGPU*>(mt);
-        s->num_materials = static_cast<int>(hs.materials.size());
-        s->fast_nodes = static_cast<int64_t>(hs.bvh.fast_nodes.size());
-        s->ref_nodes = static_cast<int64_t>(hs.bvh.ref_nodes.size());
-        s->refs = static_cast<int64_t>(hs.bvh.ref_prims.size());
-        s->bvh_depth = hs.bvh.max_depth;
-        *out = s;
-        return MCRT_OK;
+        return mcrt::scene_from_host(hs, desc->num_triangles, mcrt::scene_desc_hash(*desc), out);
     }
     catch (const std::bad_alloc&)
     {

@@ -27,7 +27,8 @@
 
 namespace mcrt {
 
-// children: c >= 0 inner node index; c < 0 leaf, first reference ~c, count in n3.z/w
+// children: c >= 0 inner node index; c < 0 leaf ~((first << 4) | count) into fast_tris
+// (count <= 15; ~0 = empty); n3.z/w repeat the counts
 struct __align__(64) FastNode
 {
     float4 n0;  // c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y

@@ -107,6 +107,49 @@ def _stream_ptr():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+def _c_desc(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = None, leaf_size: int = 4):
+    """The C description of a scene and the arrays it points into (keep them alive)."""
+    v = np.ascontiguousarray(desc.vertices, np.float32).reshape(-1, 9)
+    mid = np.ascontiguousarray(desc.material_ids, np.int32)
+    nrm = None if desc.normals is None else np.ascontiguousarray(desc.normals, np.float32).reshape(-1, 9)
+    env = None if desc.envmap is None else np.ascontiguousarray(desc.envmap, np.float32)
+    mats = desc.c_materials()
+    d = N.SceneDesc()
+    d.num_triangles = v.shape[0]
+    d.vertices = v.ctypes.data
+    d.normals = None if nrm is None else nrm.ctypes.data
+    d.material_ids = mid.ctypes.data
+    d.num_materials = len(desc.materials)
+    d.materials = mats
+    if env is not None:
+        d.env_height, d.env_width = env.shape[0], env.shape[1]
+        d.env_rgb = env.ctypes.data
+    d.leaf_size = int(leaf_size)
+    keep = [v, mid, nrm, env, mats]
+    if builder == "external":
+        t = external_tree
+        nb = np.ascontiguousarray(t["node_box"], np.float32)
+        ni = np.ascontiguousarray(t["node_info"], np.int32)
+        rp = np.ascontiguousarray(t["ref_prim"], np.int32)
+        rb = np.ascontiguousarray(t["ref_box"], np.float32)
+        tree = N.BvhTree(ni.shape[0], rp.shape[0], nb.ctypes.data, ni.ctypes.data, rp.ctypes.data, rb.ctypes.data)
+        d.builder = N.BUILD_EXTERNAL
+        d.external_tree = ctypes.pointer(tree)
+        keep += [nb, ni, rp, rb, tree]
+    else:
+        d.builder = N.BUILD_SAH
+    return d, keep
+
+
+def desc_hash(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = None, leaf_size: int = 4) -> int:
+    """mcrt_scene_desc_hash: the key a scene cache file is written under."""
+    d, keep = _c_desc(desc, builder, external_tree, leaf_size)
+    h = ctypes.c_uint64()
+    N.check(N.load().mcrt_scene_desc_hash(ctypes.byref(d), ctypes.byref(h)), "mcrt_scene_desc_hash")
+    del keep
+    return int(h.value)
+
+
 class GpuScene:
     """A finalized scene on the GPU (owns its device memory)."""
 
@@ -115,35 +158,7 @@ class GpuScene:
         lib = N.load()
         self._lib = lib
         self.desc = desc
-        v = np.ascontiguousarray(desc.vertices, np.float32).reshape(-1, 9)
-        mid = np.ascontiguousarray(desc.material_ids, np.int32)
-        nrm = None if desc.normals is None else np.ascontiguousarray(desc.normals, np.float32).reshape(-1, 9)
-        env = None if desc.envmap is None else np.ascontiguousarray(desc.envmap, np.float32)
-        mats = desc.c_materials()
-        d = N.SceneDesc()
-        d.num_triangles = v.shape[0]
-        d.vertices = v.ctypes.data
-        d.normals = None if nrm is None else nrm.ctypes.data
-        d.material_ids = mid.ctypes.data
-        d.num_materials = len(desc.materials)
-        d.materials = mats
-        if env is not None:
-            d.env_height, d.env_width = env.shape[0], env.shape[1]
-            d.env_rgb = env.ctypes.data
-        d.leaf_size = int(leaf_size)
-        keep = [v, mid, nrm, env, mats]
-        if builder == "external":
-            t = external_tree
-            nb = np.ascontiguousarray(t["node_box"], np.float32)
-            ni = np.ascontiguousarray(t["node_info"], np.int32)
-            rp = np.ascontiguousarray(t["ref_prim"], np.int32)
-            rb = np.ascontiguousarray(t["ref_box"], np.float32)
-            tree = N.BvhTree(ni.shape[0], rp.shape[0], nb.ctypes.data, ni.ctypes.data, rp.ctypes.data, rb.ctypes.data)
-            d.builder = N.BUILD_EXTERNAL
-            d.external_tree = ctypes.pointer(tree)
-            keep += [nb, ni, rp, rb, tree]
-        else:
-            d.builder = N.BUILD_SAH
+        d, keep = _c_desc(desc, builder, external_tree, leaf_size)
         h = ctypes.c_void_p()
         N.check(lib.mcrt_scene_create(ctypes.byref(d), ctypes.byref(h)), "mcrt_scene_create")
         self.handle = h
@@ -159,6 +174,39 @@ class GpuScene:
             self.close()
         except Exception:
             pass
+
+    # -- scene cache files ------------------------------------------------------------
+    def save(self, path: str) -> None:
+        """mcrt_scene_save: the prepared device scene, for GpuScene.load."""
+        N.check(self._lib.mcrt_scene_save(self.handle, str(path).encode()), "mcrt_scene_save")
+
+    @classmethod
+    def load(cls, path: str, desc: SceneDesc | None = None, **kw) -> "GpuScene":
+        """mcrt_scene_load; with `desc`, the file must have been written for that
+        description (McrtError otherwise)."""
+        lib = N.load()
+        self = cls.__new__(cls)
+        self._lib = lib
+        self.desc = desc
+        self._keep = []
+        h = ctypes.c_void_p()
+        want = 0 if desc is None else desc_hash(desc, **kw)
+        N.check(lib.mcrt_scene_load(str(path).encode(), ctypes.c_uint64(want), ctypes.byref(h)), "mcrt_scene_load")
+        self.handle = h
+        return self
+
+    @classmethod
+    def cached(cls, desc: SceneDesc, path: str, **kw) -> "GpuScene":
+        """Loads `path` when it holds this description's scene, else builds and writes it."""
+        import os
+        if os.path.exists(path):
+            try:
+                return cls.load(path, desc, **kw)
+            except N.McrtError:
+                pass
+        sc = cls(desc, **kw)
+        sc.save(path)
+        return sc
 
     def info(self) -> dict:
         a, b, c, d = N.c_int64(), N.c_int64(), N.c_int64(), N.c_int64()

@@ -102,3 +102,20 @@ def test_scenebvh_adapter_compiles_against_reference_headers(tmp_path):
     for sym in ("SceneBVH::SceneBVH", "SceneBVH::intersect", "SceneBVH::occluded", "SceneBVH::~SceneBVH"):
         assert sym in out
     assert "U mcrt_trace_closest" in out and "U mcrt_scene_create" in out
+
+
+def test_scene_description_hash_is_stable_and_sensitive(native):
+    """The key of scene cache files: equal for equal descriptions, different when any
+    input changes (host code only)."""
+    from mcrt_gb300 import scenes
+    from mcrt_gb300.scene import desc_hash
+    a = scenes.cfg0_scene()
+    h = desc_hash(a)
+    assert h == desc_hash(scenes.cfg0_scene()) and h != 0
+    assert desc_hash(a, leaf_size=2) != h
+    b = scenes.cfg0_scene()
+    b.vertices = b.vertices.copy()
+    b.vertices.reshape(-1)[5] += 1e-6
+    assert desc_hash(b) != h
+    c = scenes.cfg0_scene(sphere_level=3)
+    assert desc_hash(c) != h
