@@ -193,6 +193,15 @@ const char* mcrt_last_error(void);
  * the emitter and environment-map sampling tables and uploads everything. */
 int mcrt_scene_create(const mcrt_scene_desc* desc, mcrt_scene** out_scene);
 int mcrt_scene_destroy(mcrt_scene* scene);
+/* The library's own BVH builder (binned SAH over object splits, multithreaded; host only,
+ * no GPU needed), returned in the mcrt_bvh_tree form of the reference SplitBVH dump.  Call
+ * with node_box == NULL to get *num_nodes / *num_refs, then with arrays of those sizes
+ * (node_box [6 * nodes], node_info [6 * nodes], ref_prim [refs], ref_box [6 * refs]).
+ * leaf_size: max references per leaf (1..15, 0 -> 4).  Replaces SplitBVH::SplitBVH
+ * (splitbvh.cpp:1410-1625) for callers that build trees themselves. */
+int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int32_t leaf_size, int32_t* num_nodes,
+                   int32_t* num_refs, float* node_box, int32_t* node_info, int32_t* ref_prim, float* ref_box);
+
 /* Scene cache files (no reference counterpart: the reference rebuilds its SplitBVH, 58 s
  * at 1.3 M triangles, on every run).  mcrt_scene_save writes the prepared device scene
  * (node layouts, leaf triangles, shading, emitter and environment tables) with the hash of

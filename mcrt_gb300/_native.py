@@ -117,6 +117,8 @@ EXPORTS = {
     "mcrt_render_batch": (c_int32, [c_int32, ctypes.POINTER(c_void_p), ctypes.POINTER(Camera),
                                     ctypes.POINTER(RenderParams), ctypes.POINTER(c_void_p),
                                     ctypes.POINTER(RenderStats), c_void_p]),
+    "mcrt_build_bvh": (c_int32, [c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), ctypes.POINTER(c_int32),
+                                 c_void_p, c_void_p, c_void_p, c_void_p]),
     "mcrt_scene_desc_hash": (c_int32, [ctypes.POINTER(SceneDesc), ctypes.POINTER(ctypes.c_uint64)]),
     "mcrt_scene_save": (c_int32, [c_void_p, ctypes.c_char_p]),
     "mcrt_scene_load": (c_int32, [ctypes.c_char_p, ctypes.c_uint64, ctypes.POINTER(c_void_p)]),

@@ -11,6 +11,7 @@
 // The description hash (mcrt_scene_desc_hash) covers every input of the scene and the
 // format version, so a cache written for another mesh, material table, environment map,
 // leaf size or builder is recognised and rejected by mcrt_scene_load.
+#include <climits>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -342,5 +343,44 @@ extern "C" int mcrt_scene_load(const char* path, uint64_t expected_hash, mcrt_sc
     catch (...)
     {
         return set_error(MCRT_ERR_INTERNAL, "unexpected exception in mcrt_scene_load");
+    }
+}
+
+extern "C" int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int32_t leaf_size, int32_t* num_nodes,
+                              int32_t* num_refs, float* node_box, int32_t* node_info, int32_t* ref_prim,
+                              float* ref_box)
+{
+    if (!vertices || num_triangles <= 0 || !num_nodes || !num_refs)
+        return set_error(MCRT_ERR_INVALID_ARGUMENT, "mcrt_build_bvh: null argument or no triangles");
+    if (leaf_size < 0 || leaf_size > 15) return set_error(MCRT_ERR_INVALID_ARGUMENT, "leaf_size must be in [0, 15]");
+    if (num_triangles > (int64_t(1) << 30)) return set_error(MCRT_ERR_INVALID_ARGUMENT, "too many triangles");
+    try
+    {
+        BinaryTree t;
+        build_sah_tree(vertices, num_triangles, leaf_size > 0 ? leaf_size : 4, t);
+        const int64_t nodes = static_cast<int64_t>(t.node_info.size() / 6);
+        const int64_t refs = static_cast<int64_t>(t.ref_prim.size());
+        if (nodes > INT32_MAX || refs > INT32_MAX) return set_error(MCRT_ERR_INVALID_ARGUMENT, "tree too large");
+        if (node_box)
+        {
+            if (*num_nodes < nodes || *num_refs < refs || !node_info || !ref_prim || !ref_box)
+                return set_error(MCRT_ERR_INVALID_ARGUMENT, "mcrt_build_bvh: output arrays too small or null");
+            std::memcpy(node_box, t.node_box.data(), sizeof(float) * t.node_box.size());
+            std::memcpy(node_info, t.node_info.data(), sizeof(int32_t) * t.node_info.size());
+            std::memcpy(ref_prim, t.ref_prim.data(), sizeof(int32_t) * t.ref_prim.size());
+            std::memcpy(ref_box, t.ref_box.data(), sizeof(float) * t.ref_box.size());
+        }
+        *num_nodes = static_cast<int32_t>(nodes);
+        *num_refs = static_cast<int32_t>(refs);
+        if (t.root != 0) return set_error(MCRT_ERR_INTERNAL, "builder root is not node 0");
+        return MCRT_OK;
+    }
+    catch (const std::bad_alloc&)
+    {
+        return set_error(MCRT_ERR_OUT_OF_MEMORY, "mcrt_build_bvh: host allocation failed");
+    }
+    catch (...)
+    {
+        return set_error(MCRT_ERR_INTERNAL, "unexpected exception in mcrt_build_bvh");
     }
 }

@@ -141,6 +141,35 @@ def _c_desc(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = 
     return d, keep
 
 
+def build_bvh(vertices, leaf_size: int = 4) -> dict:
+    """mcrt_build_bvh: the library's binned-SAH tree of (n, 9) triangle vertices, in the
+    form of a reference SplitBVH dump (node_box, node_info, ref_prim, ref_box; root 0)."""
+    lib = N.load()
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
+    nn, nr = ctypes.c_int32(), ctypes.c_int32()
+    N.check(lib.mcrt_build_bvh(v.ctypes.data, v.shape[0], int(leaf_size), ctypes.byref(nn), ctypes.byref(nr),
+                               None, None, None, None), "mcrt_build_bvh")
+    nb = np.zeros((nn.value, 6), np.float32)
+    ni = np.zeros((nn.value, 6), np.int32)
+    rp = np.zeros(nr.value, np.int32)
+    rb = np.zeros((nr.value, 6), np.float32)
+    N.check(lib.mcrt_build_bvh(v.ctypes.data, v.shape[0], int(leaf_size), ctypes.byref(nn), ctypes.byref(nr),
+                               nb.ctypes.data, ni.ctypes.data, rp.ctypes.data, rb.ctypes.data), "mcrt_build_bvh")
+    return {"node_box": nb, "node_info": ni, "ref_prim": rp, "ref_box": rb}
+
+
+def sah_cost(tree: dict, c_node: float = 1.0, c_tri: float = 1.0, root: int = 0) -> float:
+    """SAH cost of a binary tree in mcrt_bvh_tree form: sum over inner nodes of
+    c_node * area / root area plus over leaves of c_tri * references * area / root area
+    (areas as AABB::surfaceAreaCost, aabb.cpp:276-282)."""
+    nb = np.asarray(tree["node_box"], np.float64).reshape(-1, 6)
+    ni = np.asarray(tree["node_info"]).reshape(-1, 6)
+    e = nb[:, 3:] - nb[:, :3]
+    area = e[:, 0] * e[:, 1] + e[:, 1] * e[:, 2] + e[:, 0] * e[:, 2]
+    leaf = ni[:, 0] != 0
+    return float((c_node * area[~leaf].sum() + c_tri * (area[leaf] * ni[leaf, 5]).sum()) / area[root])
+
+
 def desc_hash(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = None, leaf_size: int = 4) -> int:
     """mcrt_scene_desc_hash: the key a scene cache file is written under."""
     d, keep = _c_desc(desc, builder, external_tree, leaf_size)
