@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define MCRT_ABI_VERSION 2
+#define MCRT_ABI_VERSION 3
 
 /* status codes */
 #define MCRT_OK 0
@@ -50,6 +50,11 @@ extern "C" {
 #define MCRT_MAT_REFR 3 /* smooth dielectric, exact Fresnel (bsdf.cpp:319-440) */
 #define MCRT_MAT_GLSY 4 /* Phong lobe, exponent 25 (bsdf.cpp:209-301) */
 #define MCRT_MAT_GGX 8  /* GGX conductor (new: Walter 2007, Heitz 2018, Schlick F0 = color) */
+/* flag OR'd into a material type: the vertex shades with the consistent normal
+ * (TriangleObject::consistentNormal, triangle.cpp:149-182; Reshetov et al. 2010) instead of
+ * the interpolated vertex normal, so mirror reflections never leave through the surface;
+ * needs the per-corner alphas of mcrt_scene_desc::vertex_alpha (or derived, see there) */
+#define MCRT_MAT_CONSISTENT 0x100
 
 typedef struct mcrt_material {
     int32_t type;           /* MCRT_MAT_* */
@@ -91,6 +96,10 @@ typedef struct mcrt_scene_desc {
     int32_t              builder; /* MCRT_BUILD_* */
     int32_t              leaf_size; /* own builder: max triangles per leaf (0 -> 4) */
     const mcrt_bvh_tree* external_tree;
+    /* [num_triangles][3] per-corner alpha for MCRT_MAT_CONSISTENT materials
+     * (TriangleObject::m_vertex_alpha as Mesh::genNormals computes it, mesh.cpp:92-115);
+     * NULL -> mcrt_vertex_alpha of the triangles (vertices welded by position) */
+    const float*         vertex_alpha;
 } mcrt_scene_desc;
 
 typedef struct mcrt_scene mcrt_scene;
@@ -193,6 +202,12 @@ const char* mcrt_last_error(void);
  * the emitter and environment-map sampling tables and uploads everything. */
 int mcrt_scene_create(const mcrt_scene_desc* desc, mcrt_scene** out_scene);
 int mcrt_scene_destroy(mcrt_scene* scene);
+/* Per-corner alpha of consistent normals for a triangle soup: Mesh::genNormals
+ * (mesh.cpp:66-116) with the corners welded by exact position: alpha = the angle of the
+ * smallest cosine between the corner's vertex normal and the unit normals of the faces
+ * sharing its position, times 1 + 0.03632 (1 - cos)^2.  out: [num_triangles][3]. */
+int mcrt_vertex_alpha(const float* vertices, const float* normals, int64_t num_triangles, float* out);
+
 /* The library's own BVH builder (binned SAH over object splits, multithreaded; host only,
  * no GPU needed), returned in the mcrt_bvh_tree form of the reference SplitBVH dump.  Call
  * with node_box == NULL to get *num_nodes / *num_refs, then with arrays of those sizes

@@ -41,6 +41,7 @@ SCHEDULE_STREAM = 0
 SCHEDULE_WAVES = 1
 BUILD_SAH = 0
 BUILD_EXTERNAL = 1
+MAT_CONSISTENT = 0x100
 
 
 class Material(ctypes.Structure):
@@ -57,7 +58,7 @@ class SceneDesc(ctypes.Structure):
     _fields_ = [("num_triangles", c_int64), ("vertices", c_void_p), ("normals", c_void_p),
                 ("material_ids", c_void_p), ("num_materials", c_int32), ("materials", ctypes.POINTER(Material)),
                 ("env_width", c_int32), ("env_height", c_int32), ("env_rgb", c_void_p), ("builder", c_int32),
-                ("leaf_size", c_int32), ("external_tree", ctypes.POINTER(BvhTree))]
+                ("leaf_size", c_int32), ("external_tree", ctypes.POINTER(BvhTree)), ("vertex_alpha", c_void_p)]
 
 
 class Ray(ctypes.Structure):
@@ -117,6 +118,7 @@ EXPORTS = {
     "mcrt_render_batch": (c_int32, [c_int32, ctypes.POINTER(c_void_p), ctypes.POINTER(Camera),
                                     ctypes.POINTER(RenderParams), ctypes.POINTER(c_void_p),
                                     ctypes.POINTER(RenderStats), c_void_p]),
+    "mcrt_vertex_alpha": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),
     "mcrt_build_bvh": (c_int32, [c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), ctypes.POINTER(c_int32),
                                  c_void_p, c_void_p, c_void_p, c_void_p]),
     "mcrt_scene_desc_hash": (c_int32, [ctypes.POINTER(SceneDesc), ctypes.POINTER(ctypes.c_uint64)]),

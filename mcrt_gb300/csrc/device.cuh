@@ -483,6 +483,7 @@ __device__ __forceinline__ float3 shading_normal(const SceneView& s, int prim, f
 struct Mat
 {
     int    type;
+    bool   consistent;  // MCRT_MAT_CONSISTENT: shade with the consistent normal
     float3 color;
     float  roughness, ior;
     int    albedo_param, emission_param;
@@ -492,7 +493,8 @@ __device__ __forceinline__ Mat load_mat(const SceneView& s, int m)
 {
     MaterialGPU g = s.materials[m];
     Mat         r;
-    r.type = g.type;
+    r.type = g.type & 0xff;
+    r.consistent = (g.type & 0x100) != 0;
     r.color = mk(g.r, g.g, g.b);
     r.roughness = g.roughness;
     r.ior = g.ior;
@@ -502,6 +504,33 @@ __device__ __forceinline__ Mat load_mat(const SceneView& s, int m)
 }
 
 constexpr int MAT_LGHT = 0, MAT_DIFF = 1, MAT_SPEC = 2, MAT_REFR = 3, MAT_GLSY = 4, MAT_GGX = 8;
+
+// TriangleObject::consistentNormal (triangle.cpp:149-182; Reshetov, Soupikov, Kapustin
+// 2010): from the interpolated normal np and the interpolated vertex alpha, the normal
+// about which wi reflects to a direction that stays above the surface.  Float operations
+// in the reference's order, no contraction.
+__device__ __forceinline__ float3 consistent_normal(const SceneView& s, int prim, float u, float v, float3 wi,
+                                                    float3 np)
+{
+    const float4 al = __ldg(&s.prim_alpha[prim]);
+    const float  w0 = __fsub_rn(__fsub_rn(1.0f, u), v);
+    const float  alpha = __fadd_rn(__fadd_rn(__fmul_rn(w0, al.x), __fmul_rn(u, al.y)), __fmul_rn(v, al.z));
+    const float  k = 2.0f / kPi;
+    const float  t = __fsub_rn(1.0f, __fmul_rn(k, alpha));
+    const float  q = __fdiv_rn(__fmul_rn(t, t),
+                              __fadd_rn(1.0f, __fmul_rn(__fmul_rn(2.0f, __fsub_rn(1.0f, k)), alpha)));
+    const float  b = __fadd_rn(__fadd_rn(__fmul_rn(wi.x, np.x), __fmul_rn(wi.y, np.y)), __fmul_rn(wi.z, np.z));
+    const float  g = __fadd_rn(1.0f, __fmul_rn(q, __fsub_rn(b, 1.0f)));
+    const float  rho = __fsqrt_rn(__fdiv_rn(__fmul_rn(q, __fadd_rn(1.0f, g)), __fadd_rn(1.0f, b)));
+    const float  c = __fadd_rn(g, __fmul_rn(rho, b));
+    const float3 r = mk(__fsub_rn(__fmul_rn(c, np.x), __fmul_rn(rho, wi.x)),
+                        __fsub_rn(__fmul_rn(c, np.y), __fmul_rn(rho, wi.y)),
+                        __fsub_rn(__fmul_rn(c, np.z), __fmul_rn(rho, wi.z)));
+    const float3 h = mk(__fadd_rn(wi.x, r.x), __fadd_rn(wi.y, r.y), __fadd_rn(wi.z, r.z));
+    const float  inv = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(h.x, h.x), __fmul_rn(h.y, h.y)),
+                                                             __fmul_rn(h.z, h.z))));
+    return mk(__fmul_rn(h.x, inv), __fmul_rn(h.y, inv), __fmul_rn(h.z, inv));
+}
 __device__ __forceinline__ bool does_nee(int type) { return type == MAT_DIFF || type == MAT_GGX; }
 
 // OrthonormalFrame::setFromNormal (geometry.cpp:74-105; Duff et al. 2017)

@@ -52,6 +52,7 @@ struct HostScene
     std::vector<float>       env_cond;
     std::vector<int32_t>     env_guide_m;  // kEnvGuideM + 1 entries
     std::vector<int32_t>     env_guide_c;  // per column kEnvGuideC + 1 entries
+    std::vector<float4>      prim_alpha;   // per prim consistent-normal alphas (empty: none used)
     float                    env_norm = 0.f;
 };
 

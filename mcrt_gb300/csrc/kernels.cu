@@ -545,6 +545,7 @@ __global__ void __launch_bounds__(128, 8) k_shade(WaveArgs a, int p)
                 int    matid;
                 float3 ns = shading_normal(S, prim, hh.y, hh.z, matid);
                 Mat    m = load_mat(S, matid);
+                if (m.consistent) ns = consistent_normal(S, prim, hh.y, hh.z, -d, ns);
                 phit = o + d * hh.x;
                 if (m.type == MAT_LGHT)
                 {
@@ -808,6 +809,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_adjoint(AdjointArgs a)
             int    matid;
             float3 ns = shading_normal(S, h.prim, h.u, h.v, matid);
             Mat    m = load_mat(S, matid);
+            if (m.consistent) ns = consistent_normal(S, h.prim, h.u, h.v, -d, ns);
             float3 phit = o + d * h.t;
             if (m.type == MAT_LGHT)
             {
@@ -1784,6 +1786,7 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
     const float*       ec;
     const int*         egm;
     const int*         egc;
+    const float4*      pa;
     up(hs.bvh.fast_nodes, &fn);
     up(hs.bvh.fast_tris, &ft);
     up(hs.bvh.ref_nodes, &rn);
@@ -1798,6 +1801,7 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
     up(hs.env_cond, &ec);
     up(hs.env_guide_m, &egm);
     up(hs.env_guide_c, &egc);
+    up(hs.prim_alpha, &pa);
     if (rc != MCRT_OK)
     {
         std::string msg = g_err;
@@ -1805,6 +1809,7 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
         return fail(rc, msg);
     }
     SceneView& v = s->view;
+    v.prim_alpha = pa;
     v.fast_nodes = fn;
     v.fast_tris = ft;
     v.ref_nodes = rn;
@@ -1839,7 +1844,7 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
 // downloads a scene's prepared arrays (the inverse of scene_from_host)
 int scene_to_host(const mcrt_scene* s, HostScene& hs, int64_t& num_tris, uint64_t& desc_hash)
 {
-    if (s->array_bytes.size() != 14) return fail(MCRT_ERR_INTERNAL, "scene arrays not recorded");
+    if (s->array_bytes.size() != 15) return fail(MCRT_ERR_INTERNAL, "scene arrays not recorded");
     CK(cudaSetDevice(s->device));
     const SceneView& v = s->view;
     int              k = 0, rc = MCRT_OK;
@@ -1866,6 +1871,7 @@ int scene_to_host(const mcrt_scene* s, HostScene& hs, int64_t& num_tris, uint64_
     down(hs.env_cond, v.env_cond);
     down(hs.env_guide_m, v.env_guide_m);
     down(hs.env_guide_c, v.env_guide_c);
+    down(hs.prim_alpha, v.prim_alpha);
     hs.light_area = v.light_area;
     hs.env_w = v.env_w;
     hs.env_h = v.env_h;

@@ -89,6 +89,7 @@ struct SceneView
     const float*       env_cond;      // W*H: per column, H-entry CDF (column-major)
     const int*         env_guide_m;   // kEnvGuideM + 1: lower bound of g / kEnvGuideM in env_marginal
     const int*         env_guide_c;   // W*(kEnvGuideC + 1): the same per column of env_cond
+    const float4*      prim_alpha;    // per prim: consistent-normal alphas of a, b, c (or null)
     int                num_lights;
     float              light_area;
     int                env_w, env_h;

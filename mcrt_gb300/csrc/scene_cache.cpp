@@ -3,9 +3,9 @@
 // without running the builder, the flattener or the table construction.
 //
 // Format (little-endian, version kFormat):
-//   "MCRTSCN\0"  u32 format  u32 array count (14)  u64 description hash  i64 triangles
+//   "MCRTSCN\0"  u32 format  u32 array count (15)  u64 description hash  i64 triangles
 //   f32 light_area  f32 env_norm  i32 env_w  i32 env_h  i32 bvh_depth  i32 0
-//   14 x { u32 element size, u32 0, i64 bytes }  -- the arrays of scene_from_host, in order
+//   15 x { u32 element size, u32 0, i64 bytes }  -- the arrays of scene_from_host, in order
 //   the arrays' bytes, in order
 //   u64 checksum (FNV-1a 64 over 64-bit words) of everything before it
 // The description hash (mcrt_scene_desc_hash) covers every input of the scene and the
@@ -25,8 +25,8 @@
 namespace mcrt {
 namespace {
 
-constexpr uint32_t kFormat = 1;
-constexpr int      kArrays = 14;
+constexpr uint32_t kFormat = 2;
+constexpr int      kArrays = 15;
 const char         kMagic[8] = {'M', 'C', 'R', 'T', 'S', 'C', 'N', '\0'};
 
 // FNV-1a 64 over little-endian 64-bit words (remaining bytes one at a time): the hash of
@@ -61,7 +61,8 @@ struct Fnv
 // element sizes of the arrays of HostScene in scene_from_host's order
 const uint32_t kElem[kArrays] = {sizeof(FastNode), sizeof(float4), sizeof(RefNode),     sizeof(RefPrim), sizeof(float4),
                                  sizeof(float4),   sizeof(int32_t), sizeof(LightGPU),   sizeof(MaterialGPU),
-                                 sizeof(float4),   sizeof(float),   sizeof(float),      sizeof(int32_t), sizeof(int32_t)};
+                                 sizeof(float4),   sizeof(float),   sizeof(float),      sizeof(int32_t), sizeof(int32_t),
+                                 sizeof(float4)};
 
 struct Header
 {
@@ -97,6 +98,7 @@ void for_each_array(HostScene& hs, F&& f)
     f(hs.env_cond);
     f(hs.env_guide_m);
     f(hs.env_guide_c);
+    f(hs.prim_alpha);
 }
 
 inline int32_t ibits(float f)
@@ -157,6 +159,8 @@ std::string validate(const HostScene& hs, int64_t num_tris)
         if (l < -1 || l >= lights) return "emitter index out of range";
     for (const LightGPU& l : hs.lights)
         if (l.prim < 0 || l.prim >= num_tris) return "emitter primitive out of range";
+    if (!hs.prim_alpha.empty() && hs.prim_alpha.size() != static_cast<size_t>(num_tris))
+        return "consistent-normal table size";
     if (hs.env_w > 0)
     {
         const size_t W = static_cast<size_t>(hs.env_w), H = static_cast<size_t>(hs.env_h);
@@ -199,6 +203,9 @@ uint64_t scene_desc_hash(const mcrt_scene_desc& d)
     h.add_value(d.env_height);
     if (d.env_rgb && d.env_width > 0 && d.env_height > 0)
         h.add(d.env_rgb, sizeof(float) * 3 * static_cast<size_t>(d.env_width) * d.env_height);
+    const int32_t has_alpha = d.vertex_alpha ? 1 : 0;
+    h.add_value(has_alpha);
+    if (d.vertex_alpha) h.add(d.vertex_alpha, sizeof(float) * 3 * static_cast<size_t>(d.num_triangles));
     h.add_value(d.builder);
     const int32_t leaf = d.leaf_size > 0 ? d.leaf_size : 4;
     h.add_value(leaf);

@@ -9,10 +9,12 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/mcrt_gb300.h"
 #include "host.h"
+#include "wavefront.h"
 
 namespace mcrt {
 namespace {
@@ -42,6 +44,63 @@ inline float  ibits(int32_t i)
 }
 
 // DiscreteSampler::update: pdf = data * (1 / sum), cdf = running float sum
+// Mesh::genNormals' vertex alpha (mesh.cpp:92-115) on a triangle soup: corners welded by
+// exact position; per corner the smallest cosine between its normal and the unit normals of
+// the faces sharing its position (1 if larger), then acos(a) * (1 + 0.03632 (1 - a)^2)
+// (acos in double, as the reference's unqualified call on a float).
+void vertex_alpha_soup(const float* verts, const float* normals, int64_t n, float* out)
+{
+    struct Key
+    {
+        uint32_t x, y, z;
+        bool     operator==(const Key& o) const { return x == o.x && y == o.y && z == o.z; }
+    };
+    struct KeyHash
+    {
+        size_t operator()(const Key& k) const
+        {
+            uint64_t h = k.x * 0x9E3779B97F4A7C15ull;
+            h ^= (h >> 29) ^ (k.y * 0xBF58476D1CE4E5B9ull);
+            h ^= (h >> 31) ^ (k.z * 0x94D049BB133111EBull);
+            return static_cast<size_t>(h ^ (h >> 32));
+        }
+    };
+    auto bits = [](float f) {
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        return u;
+    };
+    std::vector<V> face(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i)
+    {
+        const V a = ld(verts + 9 * i), b = ld(verts + 9 * i + 3), c = ld(verts + 9 * i + 6);
+        face[i] = normalize(cross(sub(b, a), sub(c, a)));
+    }
+    std::unordered_map<Key, std::vector<int64_t>, KeyHash> share;  // position -> faces
+    share.reserve(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i)
+        for (int c = 0; c < 3; ++c)
+        {
+            const float* p = verts + 9 * i + 3 * c;
+            share[Key{bits(p[0]), bits(p[1]), bits(p[2])}].push_back(i);
+        }
+    const float w = 0.03632f;
+    for (int64_t i = 0; i < n; ++i)
+        for (int c = 0; c < 3; ++c)
+        {
+            const float* p = verts + 9 * i + 3 * c;
+            const V      nv = ld(normals + 9 * i + 3 * c);
+            float        a = 1.f;
+            for (int64_t f : share[Key{bits(p[0]), bits(p[1]), bits(p[2])}])
+            {
+                const float dt = face[f].x * nv.x + face[f].y * nv.y + face[f].z * nv.z;
+                a = a < dt ? a : dt;  // f_min
+            }
+            out[3 * i + c] = static_cast<float>(std::acos(static_cast<double>(a)) *
+                                                static_cast<double>(1 + w * ((1 - a) * (1 - a))));
+        }
+}
+
 // first index i of cdf[0..n-1] with cdf[i] >= r, or n - 1 (the device search, same loop)
 int lower_bound_cdf_host(const float* cdf, int n, float r)
 {
@@ -84,12 +143,16 @@ std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs)
     for (int64_t i = 0; i < n; ++i)
         if (d.material_ids[i] < 0 || d.material_ids[i] >= d.num_materials) return "material id out of range";
     hs.materials.resize(d.num_materials);
+    bool any_consistent = false;
     for (int m = 0; m < d.num_materials; ++m)
     {
         const mcrt_material& s = d.materials[m];
-        if (s.type != MCRT_MAT_LGHT && s.type != MCRT_MAT_DIFF && s.type != MCRT_MAT_SPEC && s.type != MCRT_MAT_REFR &&
-            s.type != MCRT_MAT_GLSY && s.type != MCRT_MAT_GGX)
+        const int            base = s.type & 0xff;
+        if ((s.type & ~(0xff | MCRT_MAT_CONSISTENT)) != 0 ||
+            (base != MCRT_MAT_LGHT && base != MCRT_MAT_DIFF && base != MCRT_MAT_SPEC && base != MCRT_MAT_REFR &&
+             base != MCRT_MAT_GLSY && base != MCRT_MAT_GGX))
             return "unknown material type";
+        if (s.type & MCRT_MAT_CONSISTENT) any_consistent = true;
         MaterialGPU& g = hs.materials[m];
         g.type = s.type;
         g.r = s.color[0];
@@ -153,7 +216,7 @@ std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs)
         hs.prim_shade[3 * i + 0] = f4(na, ibits(d.material_ids[i]));
         hs.prim_shade[3 * i + 1] = f4(nb, 0.f);
         hs.prim_shade[3 * i + 2] = f4(nc, 0.f);
-        if (d.materials[d.material_ids[i]].type == MCRT_MAT_LGHT)
+        if ((d.materials[d.material_ids[i]].type & 0xff) == MCRT_MAT_LGHT)
         {
             hs.light_of[i] = static_cast<int32_t>(hs.lights.size());
             LightGPU l;
@@ -178,6 +241,33 @@ std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs)
         hs.light_area = la;
     }
 
+    // per-corner alphas of consistent normals, only when a material asks for them
+    if (any_consistent)
+    {
+        std::vector<float> alpha;
+        const float*       src = d.vertex_alpha;
+        if (!src)
+        {
+            alpha.resize(9 * static_cast<size_t>(n) / 3);
+            std::vector<float> nrm;
+            if (!d.normals)
+            {
+                nrm.resize(9 * static_cast<size_t>(n));
+                for (int64_t i = 0; i < n; ++i)
+                    for (int c = 0; c < 3; ++c)
+                    {
+                        const float4& q = hs.prim_shade[3 * i + c];
+                        nrm[9 * i + 3 * c + 0] = q.x;
+                        nrm[9 * i + 3 * c + 1] = q.y;
+                        nrm[9 * i + 3 * c + 2] = q.z;
+                    }
+            }
+            vertex_alpha_soup(d.vertices, d.normals ? d.normals : nrm.data(), n, alpha.data());
+            src = alpha.data();
+        }
+        hs.prim_alpha.resize(static_cast<size_t>(n));
+        for (int64_t i = 0; i < n; ++i) hs.prim_alpha[i] = float4{src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.f};
+    }
     // environment map
     if (d.env_rgb && d.env_width > 0 && d.env_height > 0)
     {
@@ -233,3 +323,18 @@ std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs)
 }
 
 }  // namespace mcrt
+
+extern "C" int mcrt_vertex_alpha(const float* vertices, const float* normals, int64_t num_triangles, float* out)
+{
+    if (!vertices || !normals || !out || num_triangles <= 0) return mcrt::set_error(MCRT_ERR_INVALID_ARGUMENT,
+                                                                                 "mcrt_vertex_alpha: null argument");
+    try
+    {
+        mcrt::vertex_alpha_soup(vertices, normals, num_triangles, out);
+        return MCRT_OK;
+    }
+    catch (...)
+    {
+        return mcrt::set_error(MCRT_ERR_INTERNAL, "unexpected exception in mcrt_vertex_alpha");
+    }
+}

@@ -20,6 +20,7 @@ from . import _native as N
 
 # MaterialType (src/core/material.h:7) plus the GGX conductor
 LGHT, DIFF, SPEC, REFR, GLSY, GGX = 0, 1, 2, 3, 4, 8
+CONSISTENT = 0x100  # OR'd into a type: shade with the consistent normal (TriangleObject::consistentNormal)
 
 
 @dataclass
@@ -64,6 +65,7 @@ class SceneDesc:
     materials: list                      # list[Material]
     normals: np.ndarray | None = None    # (n, 9) float32: na, nb, nc
     envmap: np.ndarray | None = None     # (H, W, 3) float32, top row first
+    vertex_alpha: np.ndarray | None = None  # (n, 3) float32 consistent-normal alphas (None: derived)
     name: str = ""
     extra: dict = field(default_factory=dict)
 
@@ -125,7 +127,9 @@ def _c_desc(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = 
         d.env_height, d.env_width = env.shape[0], env.shape[1]
         d.env_rgb = env.ctypes.data
     d.leaf_size = int(leaf_size)
-    keep = [v, mid, nrm, env, mats]
+    alpha = None if desc.vertex_alpha is None else np.ascontiguousarray(desc.vertex_alpha, np.float32).reshape(-1, 3)
+    d.vertex_alpha = None if alpha is None else alpha.ctypes.data
+    keep = [v, mid, nrm, env, mats, alpha]
     if builder == "external":
         t = external_tree
         nb = np.ascontiguousarray(t["node_box"], np.float32)
@@ -139,6 +143,16 @@ def _c_desc(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = 
     else:
         d.builder = N.BUILD_SAH
     return d, keep
+
+
+def vertex_alpha(vertices, normals) -> np.ndarray:
+    """mcrt_vertex_alpha: per-corner consistent-normal alphas (n, 3) of a triangle soup."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
+    nrm = np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+    out = np.zeros((v.shape[0], 3), np.float32)
+    N.check(N.load().mcrt_vertex_alpha(v.ctypes.data, nrm.ctypes.data, v.shape[0], out.ctypes.data),
+            "mcrt_vertex_alpha")
+    return out
 
 
 def build_bvh(vertices, leaf_size: int = 4) -> dict:

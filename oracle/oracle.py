@@ -89,6 +89,8 @@ def load_restatement():
         lib.orc_film_ppm.restype = LL
         lib.orc_film_ppm.argtypes = [I, I, P, P, LL]
         lib.orc_film_tonemap.argtypes = [I, I, P, I, F]
+        lib.orc_scene_set_alpha.argtypes = [P, P]
+        lib.orc_consistent_normal.argtypes = [P, P, P, P, F, F, P]
         _orc = lib
     return _orc
 
@@ -141,6 +143,8 @@ def load_reference():
         lib.ref_render_cornell.restype = I
         lib.ref_render_cornell.argtypes = [I, I, I, I, I, I, P, P, P, P]
         lib.ref_film_dump.argtypes = [I, I, P, ctypes.c_char_p, I]
+        lib.ref_consistent_normal.argtypes = [P, P, P, P, F, F, P, P, P]
+        lib.ref_mesh_alpha.argtypes = [P, I, P, I, P, P]
         lib.ref_film_tonemap.argtypes = [I, I, P, I, F]
         _ref = lib
     return _ref
@@ -188,6 +192,10 @@ class OracleScene:
         self._keep = (v, n, mid, mt, mp, env)
         self.h = lib.orc_scene_create(precision, ptr(v), ptr(n), ptr(mid), len(mid), ptr(mt), ptr(mp), len(mt),
                                       ptr(env), ew, eh)
+        alpha = getattr(scene, "vertex_alpha", None)
+        if alpha is not None:
+            self._alpha = np.ascontiguousarray(alpha, np.float32)
+            lib.orc_scene_set_alpha(self.h, ptr(self._alpha))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -251,6 +251,7 @@ template <class T>
 struct Material
 {
     int   type;
+    bool  consistent = false;  // type flag 0x100: shade with TriangleObject::consistentNormal
     V3<T> color;
     T     roughness;
     T     ior;
@@ -632,9 +633,29 @@ template <class T>
 struct Tri
 {
     V3<T> a, b, c, na, nb, nc, n;
+    V3<T> alpha = V3<T>(T(1), T(1), T(1));  // TriangleObject::m_vertex_alpha
     T     area;
     int   mat;
 };
+
+// TriangleObject::consistentNormal (triangle.cpp:149-182): np = normal(u, v); the
+// reference's float constant 2 / NUM_PI (NUM_PI = float(pi))
+template <class T>
+V3<T> consistentNormalOf(const Tri<T>& t, const V3<T>& np, T u, T v, const V3<T>& wi, V3<T>* refl = nullptr,
+                         T* cos_wi = nullptr)
+{
+    const T k = T(2.0f / 3.14159265358979323846f);
+    T       alpha = (T(1) - u - v) * t.alpha.x + u * t.alpha.y + v * t.alpha.z;
+    T       s = T(1) - k * alpha;
+    T       q = (s * s) / (T(1) + T(2) * (T(1) - k) * alpha);
+    T       b = dot(wi, np);
+    T       g = T(1) + q * (b - T(1));
+    T       rho = std::sqrt(q * (T(1) + g) / (T(1) + b));
+    V3<T>   r = (g + rho * b) * np - rho * wi;
+    if (refl) *refl = r;
+    if (cos_wi) *cos_wi = std::sqrt((T(1) + (g + rho * b) * b - rho) * T(0.5));
+    return normalize(wi + r);
+}
 
 struct Node
 {
@@ -994,6 +1015,11 @@ struct Scene
         const Tri<T>& t = tris[p];
         return normalize((T(1) - u - v) * t.na + u * t.nb + v * t.nc);
     }
+
+    V3<T> consistentNormal(int p, T u, T v, const V3<T>& wi) const
+    {
+        return consistentNormalOf(tris[p], shadingNormal(p, u, v), u, v, wi);
+    }
 };
 
 // ---------------------------------------------------------------------------
@@ -1096,6 +1122,7 @@ PathOut<T> tracePath(const Scene<T>& sc, const V3<T>& o0, const V3<T>& d0, Pcg32
         const Material<T>& mat = sc.mats[tri.mat];
         V3<T>              phit = ro + rd * hit.t;
         V3<T>              nhit = sc.shadingNormal(hit.prim, hit.u, hit.v);
+        if (mat.consistent) nhit = sc.consistentNormal(hit.prim, hit.u, hit.v, -rd);
         if (mat.type == LGHT)
         {
             if (no_direct && dot(rd, nhit) < 0)
@@ -1459,7 +1486,8 @@ void fillScene(Scene<T>& sc, const float* verts, const float* normals, const int
     for (int m = 0; m < n_mats; ++m)
     {
         const float* p = mat_params + 8 * m;  // color3, roughness, ior, albedo_param, emission_param, pad
-        sc.mats[m].type = mat_types[m];
+        sc.mats[m].type = mat_types[m] & 0xff;
+        sc.mats[m].consistent = (mat_types[m] & 0x100) != 0;
         sc.mats[m].color = ld3<T>(p);
         sc.mats[m].roughness = T(p[3]);
         sc.mats[m].ior = T(p[4]);
@@ -1537,6 +1565,35 @@ void* orc_scene_create(int precision, const float* verts, const float* normals, 
 }
 
 void orc_scene_destroy(void* h) { delete static_cast<SceneAny*>(h); }
+
+// per-corner consistent-normal alphas, [n_tris][3]
+void orc_scene_set_alpha(void* h, const float* alpha)
+{
+    SceneAny* s = static_cast<SceneAny*>(h);
+    if (s->precision == 64)
+        for (size_t i = 0; i < s->d->tris.size(); ++i) s->d->tris[i].alpha = ld3<double>(alpha + 3 * i);
+    else
+        for (size_t i = 0; i < s->f->tris.size(); ++i) s->f->tris[i].alpha = ld3<float>(alpha + 3 * i);
+}
+
+// TriangleObject::consistentNormal of one triangle (float): out = normal, reflection, cos
+void orc_consistent_normal(const float* abc, const float* nabc, const float* alpha3, const float* wi, float u,
+                           float v, float* out)
+{
+    Tri<float> t;
+    t.a = ld3<float>(abc);
+    t.b = ld3<float>(abc + 3);
+    t.c = ld3<float>(abc + 6);
+    t.na = ld3<float>(nabc);
+    t.nb = ld3<float>(nabc + 3);
+    t.nc = ld3<float>(nabc + 6);
+    t.alpha = ld3<float>(alpha3);
+    const V3<float> np = normalize((1.0f - u - v) * t.na + u * t.nb + v * t.nc);
+    V3<float>       r;
+    float           c = 0.f;
+    const V3<float> n = consistentNormalOf(t, np, u, v, ld3<float>(wi), &r, &c);
+    out[0] = n.x, out[1] = n.y, out[2] = n.z, out[3] = r.x, out[4] = r.y, out[5] = r.z, out[6] = c;
+}
 
 }  // extern "C"
 

@@ -546,3 +546,31 @@ extern "C" void ref_film_tonemap(int w, int h, float* rgb, int mode, float gamma
         fb.tonemapReinhard();
     read_fb(fb, w, h, rgb);
 }
+
+// --- consistent normals (Reshetov et al. 2010): TriangleObject::consistentNormal
+// (triangle.cpp:149-182) and the per-vertex alpha of Mesh::genNormals (mesh.cpp:66-116) --
+extern "C" void ref_consistent_normal(const float* abc, const float* nabc, const float* alpha3, const float* wi,
+                                      float u, float v, float* nc_out, float* refl_out, float* cos_out)
+{
+    TriangleObject t(v3(abc), v3(abc + 3), v3(abc + 6), v3(nabc), v3(nabc + 3), v3(nabc + 6));
+    t.setVertexAlpha(v3(alpha3));
+    vec3  r;
+    float c = 0.f;
+    put3(nc_out, t.consistentNormal(v3(wi), u, v, &r, &c));
+    put3(refl_out, r);
+    *cos_out = c;
+}
+
+extern "C" void ref_mesh_alpha(const float* verts, int nv, const int* faces, int nf, float* normals_out,
+                               float* alpha_out)
+{
+    Mesh m;
+    for (int i = 0; i < nv; ++i) m.m_verts.push_back(v3(verts + 3 * i));
+    for (int i = 0; i < nf; ++i) m.m_faces.push_back(int3(faces[3 * i], faces[3 * i + 1], faces[3 * i + 2]));
+    m.genNormals();
+    for (int i = 0; i < nv; ++i)
+    {
+        put3(normals_out + 3 * i, m.m_vertex_normals[i]);
+        alpha_out[i] = m.m_vertex_alpha[i];
+    }
+}

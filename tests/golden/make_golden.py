@@ -324,6 +324,39 @@ def film_fixture(ref):
     np.savez_compressed(os.path.join(OUT, "ref_film.npz"), **out)
 
 
+def consistent_fixture(ref):
+    """TriangleObject::consistentNormal on random triangles / directions / barycentrics,
+    and Mesh::genNormals' vertex normals and alphas of an indexed displaced icosphere."""
+    rng = np.random.default_rng(44)
+    n = 2000
+    abc = rng.normal(size=(n, 9)).astype(np.float32)
+    nabc = rng.normal(size=(n, 3, 3))
+    nabc /= np.linalg.norm(nabc, axis=2, keepdims=True)
+    nabc = nabc.reshape(n, 9).astype(np.float32)
+    alpha = rng.uniform(0.0, 1.2, (n, 3)).astype(np.float32)
+    u = rng.uniform(0, 1, n).astype(np.float32)
+    v = (rng.uniform(0, 1, n) * (1 - u)).astype(np.float32)
+    wi = rng.normal(size=(n, 3))
+    wi /= np.linalg.norm(wi, axis=1, keepdims=True)
+    # keep wi on the side of the interpolated normal (as a view direction is)
+    nint = (1 - u - v)[:, None] * nabc[:, 0:3] + u[:, None] * nabc[:, 3:6] + v[:, None] * nabc[:, 6:9]
+    wi = np.where((np.sum(wi * nint, axis=1) < 0)[:, None], -wi, wi).astype(np.float32)
+    out = np.zeros((n, 7), np.float32)
+    for i in range(n):
+        nc, rf, cs = np.zeros(3, np.float32), np.zeros(3, np.float32), np.zeros(1, np.float32)
+        ref.ref_consistent_normal(ptr(abc[i]), ptr(nabc[i]), ptr(alpha[i]), ptr(wi[i]), float(u[i]), float(v[i]),
+                                  ptr(nc), ptr(rf), ptr(cs))
+        out[i, 0:3], out[i, 3:6], out[i, 6] = nc, rf, cs[0]
+    verts, faces = scenes.icosphere(2)
+    verts = (verts * (1.0 + 0.15 * rng.uniform(-1, 1, (verts.shape[0], 1)))).astype(np.float32)
+    faces = faces.astype(np.int32)
+    vn = np.zeros_like(verts)
+    va = np.zeros(verts.shape[0], np.float32)
+    ref.ref_mesh_alpha(ptr(verts), verts.shape[0], ptr(faces), faces.shape[0], ptr(vn), ptr(va))
+    np.savez_compressed(os.path.join(OUT, "ref_consistent.npz"), abc=abc, nabc=nabc, alpha=alpha, u=u, v=v, wi=wi,
+                        out=out, mesh_verts=verts, mesh_faces=faces, mesh_normals=vn, mesh_alpha=va)
+
+
 def main():
     ref = O.load_reference()
     if ref is None:
@@ -331,7 +364,11 @@ def main():
     if "--only-film" in sys.argv:
         film_fixture(ref)
         return
+    if "--only-consistent" in sys.argv:
+        consistent_fixture(ref)
+        return
     film_fixture(ref)
+    consistent_fixture(ref)
     cornell_paths_fixture(ref)  # first: the global random stream starts at its seed here
     rng = np.random.default_rng(20261203)
     # the reference's own Cornell box (demo_pt.cpp:83-414)

@@ -20,7 +20,7 @@ def test_every_declared_symbol_is_exported(native):
     assert "mcrt_render" in names and "mcrt_trace_closest" in names
     for n in names:
         assert hasattr(native, n), f"{n} declared but not exported"
-    assert native.mcrt_get_abi_version() == 2
+    assert native.mcrt_get_abi_version() == 3
 
 
 def test_null_arguments_fail_cleanly(native):
@@ -135,3 +135,15 @@ def test_own_builder_sah_cost_against_reference_trees(native):
         ours = build_bvh(g["verts"])
         assert sorted(np.unique(ours["ref_prim"])) == list(range(g["verts"].reshape(-1, 9).shape[0]))
         assert sah_cost(ours) <= lim * sah_cost(ref), name
+
+
+def test_vertex_alpha_matches_reference_mesh(native):
+    """mcrt_vertex_alpha on the triangle soup of an indexed mesh (with the reference's own
+    vertex normals) gives Mesh::genNormals' per-vertex alpha at every corner, bit for bit."""
+    from mcrt_gb300.scene import vertex_alpha
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_consistent.npz"))
+    v, f, vn, va = g["mesh_verts"], g["mesh_faces"], g["mesh_normals"], g["mesh_alpha"]
+    soup = v[f].reshape(-1, 9)
+    nrm = vn[f].reshape(-1, 9)
+    got = vertex_alpha(soup, nrm)
+    np.testing.assert_array_equal(got, va[f])
