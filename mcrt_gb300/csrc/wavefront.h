@@ -32,7 +32,7 @@ constexpr int kTraceBlock = 128;
 constexpr int kStack = 64;
 constexpr int kMaxDepth = 62;
 constexpr int64_t kMaxQueue = int64_t(1) << 27;     // rays per queue (result indices stay in int)
-constexpr int64_t kDefaultQueue = int64_t(1) << 23;  // streaming schedule default (6 GB of queues)
+constexpr int64_t kDefaultQueue = int64_t(1) << 24;  // streaming schedule default (12 GB of queues)
 
 // counters of one render
 struct Ctrl
