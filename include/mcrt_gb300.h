@@ -169,7 +169,7 @@ typedef struct mcrt_render_params {
 /* variant 0 = default policy (STACK32 when the BVH is shallow enough, REGCAP);
  * MCRT_VARIANT_EXPLICIT | bits = exactly the given bits (for tuning) */
 #define MCRT_VARIANT_STACK32 1  /* 32-entry shared-memory stacks (16 KB/block) when the BVH is shallow enough */
-#define MCRT_VARIANT_REGCAP 2   /* cap registers at 64 so 8 blocks of 128 threads fit an SM */
+#define MCRT_VARIANT_REGCAP 2   /* cap registers at 56 so 9 blocks of 128 threads fit an SM */
 #define MCRT_VARIANT_EXPLICIT 4 /* use the bits as given instead of the default policy */
 #define MCRT_VARIANT_GRIDSTRIDE 8 /* traversal kernels: static grid stride instead of warps taking
                                      32-ray batches from a counter */

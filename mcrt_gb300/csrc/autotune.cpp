@@ -3,7 +3,7 @@
 //
 // The search is two-stage, so it costs about eight probe renders (each best of two):
 //   1. traversal kernel variants at the default queue capacity: 32-entry or 64-entry
-//      shared-memory stacks, 64-register cap or none, warp batch fetch or grid stride;
+//      shared-memory stacks, 56-register cap or none, warp batch fetch or grid stride;
 //   2. queue capacities (2^21 .. 2^24 rays) with the best variant.
 // Every configuration renders the same image (the schedule never changes a path's
 // arithmetic), so only the time is compared.

@@ -482,11 +482,12 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
 // Adjoint (ADJ): emission derivatives at emitter hits (the coefficient of E), and at a
 // parameterised Lambert vertex k the - dL/dI * L_before(k) / albedo_k half of the albedo
 // derivative; the vertex's material id goes to the path's log for the other half.
-// Registers capped at 64 (8 blocks per SM; measured faster than the uncapped 80).  One
-// build only: builds under different register budgets contract multiply-adds
-// differently, and every configuration must render the same image.
+// Registers capped at 56 (9 blocks per SM).  Per cfg1 frame: uncapped (80 registers)
+// 32.4 ms, 8 blocks 26.5, 9 blocks 25.0, 10 blocks 26.3.  One build only: builds under
+// different register budgets contract multiply-adds differently, and every
+// configuration must render the same image.
 template <bool ADJ>
-__global__ void __launch_bounds__(128, 8) k_shade(WaveArgs a, int p)
+__global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];
     const Grads G = grads_begin<ADJ>(a, sgrad);
@@ -1237,17 +1238,18 @@ struct IterEnqueue
 template <class F>
 void with_variant(bool stack32, bool regcap, bool count, const F& f)
 {
+    constexpr int B = kTraceMinBlocks;
     if (stack32)
     {
         if (regcap)
-            count ? f.template run<32, true, 8>() : f.template run<32, false, 8>();
+            count ? f.template run<32, true, B>() : f.template run<32, false, B>();
         else
             count ? f.template run<32, true, 1>() : f.template run<32, false, 1>();
     }
     else
     {
         if (regcap)
-            count ? f.template run<kStack, true, 8>() : f.template run<kStack, false, 8>();
+            count ? f.template run<kStack, true, B>() : f.template run<kStack, false, B>();
         else
             count ? f.template run<kStack, true, 1>() : f.template run<kStack, false, 1>();
     }
@@ -1470,7 +1472,7 @@ int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<
 template <int STACK>
 void enqueue_adjoint_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, size_t dyn)
 {
-    enqueue_iter<STACK, false, 8, true>(a, p, ls, st, nullptr, dyn);
+    enqueue_iter<STACK, false, kTraceMinBlocks, true>(a, p, ls, st, nullptr, dyn);
 }
 
 template <int STACK>
@@ -1478,13 +1480,14 @@ int adjoint_launch_shape(size_t dyn, LaunchShape& ls)
 {
     CK(cudaFuncSetAttribute(k_regen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
     CK(cudaFuncSetAttribute(k_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
-    CK(cudaFuncSetAttribute(k_connect<STACK, false, 8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    constexpr int B = kTraceMinBlocks;
+    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             static_cast<int>(dyn)));
     const int sms = num_sms();
     int       occ_e = 0, occ_s = 0, occ_c = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_extend<STACK, false, 8>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_extend<STACK, false, B>, kTraceBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<true>, 128, dyn);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_connect<STACK, false, 8, true>, kTraceBlock, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_connect<STACK, false, B, true>, kTraceBlock, dyn);
     ls.grid_trace = sms * std::max(occ_e, 1);
     ls.grid_connect = sms * std::max(occ_c, 1);
     ls.grid_shade = sms * std::max(occ_s, 1);
@@ -1608,7 +1611,8 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     const bool stages = (p0.profile & MCRT_PROFILE_STAGES) != 0;
     const bool graph = p0.use_graph && !stages;
     // variant 0: the default policy (32-entry stacks when the tree is shallow enough,
-    // traversal registers capped for 8 blocks per SM); MCRT_VARIANT_EXPLICIT: the given bits
+    // traversal registers capped for kTraceMinBlocks blocks per SM);
+    // MCRT_VARIANT_EXPLICIT: the given bits
     const int   vb = (p0.variant & MCRT_VARIANT_EXPLICIT) ? p0.variant : (MCRT_VARIANT_STACK32 | MCRT_VARIANT_REGCAP);
     const bool  stack32 = (vb & MCRT_VARIANT_STACK32) && bvh_depth + 2 < 32;
     const bool  regcap = (vb & MCRT_VARIANT_REGCAP) != 0;
@@ -1739,12 +1743,13 @@ LaunchShape launch_shape_variant(bool stack32, bool regcap)
     LaunchShape ls;
     int         sms = num_sms();
     int         occ_t = 0, occ_s = 0;
+    constexpr int B = kTraceMinBlocks;
     if (stack32)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, regcap ? k_extend<32, false, 8> : k_extend<32, false, 1>,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, regcap ? k_extend<32, false, B> : k_extend<32, false, 1>,
                                                       kTraceBlock, 0);
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ_t, regcap ? k_extend<kStack, false, 8> : k_extend<kStack, false, 1>, kTraceBlock, 0);
+            &occ_t, regcap ? k_extend<kStack, false, B> : k_extend<kStack, false, 1>, kTraceBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<false>, 128, 0);
     ls.grid_trace = sms * std::max(occ_t, 1);
     ls.grid_connect = ls.grid_trace;

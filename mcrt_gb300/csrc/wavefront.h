@@ -30,6 +30,11 @@ namespace mcrt {
 
 constexpr int kTraceBlock = 128;
 constexpr int kStack = 64;
+// Traversal kernels under MCRT_VARIANT_REGCAP: __launch_bounds__(kTraceBlock, kTraceMinBlocks)
+// caps them at 56 registers, so 9 blocks (36 warps) fit an SM.  Measured on the cfg1 frame:
+// 8 blocks (64 registers) 52.6 / 59.9 ms extend / connect, 9 blocks 52.2 / 56.7, 10 blocks
+// (48 registers, spills) 54.4 / 57.0.
+constexpr int kTraceMinBlocks = 9;
 constexpr int kMaxDepth = 62;
 constexpr int64_t kMaxQueue = int64_t(1) << 27;     // rays per queue (result indices stay in int)
 constexpr int64_t kDefaultQueue = int64_t(1) << 24;  // streaming schedule default (12 GB of queues)
