@@ -8,6 +8,10 @@
 
 #include "layout.h"
 
+#ifndef MCRT_NODE_V8
+#define MCRT_NODE_V8 1
+#endif
+
 namespace mcrt {
 
 constexpr float kPi = 3.14159265358979323846f;
@@ -162,6 +166,31 @@ __device__ __forceinline__ bool watertight(const WatertightRay& r, float3 v0, fl
     return true;
 }
 
+// One 64-B node: two 32-B loads (ld.global.nc.v8, sm_100 and later) where 16-B loads take
+// four.  FastNode arrays are 64-B aligned (cudaMalloc'd arrays of __align__(64) nodes).
+__device__ __forceinline__ void ldg_node(const FastNode* p, float4& n0, float4& n1, float4& n2, int4& n3)
+{
+#if MCRT_NODE_V8
+    unsigned a[8], b[8];
+    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3]), "=r"(a[4]), "=r"(a[5]), "=r"(a[6]), "=r"(a[7])
+        : "l"(p));
+    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8 + 32];"
+        : "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3]), "=r"(b[4]), "=r"(b[5]), "=r"(b[6]), "=r"(b[7])
+        : "l"(p));
+    n0 = make_float4(__uint_as_float(a[0]), __uint_as_float(a[1]), __uint_as_float(a[2]), __uint_as_float(a[3]));
+    n1 = make_float4(__uint_as_float(a[4]), __uint_as_float(a[5]), __uint_as_float(a[6]), __uint_as_float(a[7]));
+    n2 = make_float4(__uint_as_float(b[0]), __uint_as_float(b[1]), __uint_as_float(b[2]), __uint_as_float(b[3]));
+    n3 = make_int4(static_cast<int>(b[4]), static_cast<int>(b[5]), static_cast<int>(b[6]), static_cast<int>(b[7]));
+#else
+    const float4* q = reinterpret_cast<const float4*>(p);
+    n0 = __ldg(q);
+    n1 = __ldg(q + 1);
+    n2 = __ldg(q + 2);
+    n3 = __ldg(reinterpret_cast<const int4*>(q + 3));
+#endif
+}
+
 // Work counters of a traversal (MCRT_PROFILE_COUNT): nodes fetched, triangles tested.
 struct TraceCount
 {
@@ -210,12 +239,10 @@ __device__ __forceinline__ bool fast_step(FastTrav& r, const FastNode* nodes, co
 {
     while (r.cur >= 0 && r.cur != kSentinel)
     {
-        const float4* np = reinterpret_cast<const float4*>(nodes + r.cur);
         if (COUNT) cnt->nodes++;
-        float4 n0 = __ldg(np + 0);
-        float4 n1 = __ldg(np + 1);
-        float4 n2 = __ldg(np + 2);
-        int4   n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+        float4 n0, n1, n2;
+        int4   n3;
+        ldg_node(nodes + r.cur, n0, n1, n2, n3);
         float  c0lx = n0.x * r.inv.x - r.ood.x, c0hx = n0.y * r.inv.x - r.ood.x;
         float  c0ly = n0.z * r.inv.y - r.ood.y, c0hy = n0.w * r.inv.y - r.ood.y;
         float  c0lz = n2.x * r.inv.z - r.ood.z, c0hz = n2.y * r.inv.z - r.ood.z;
