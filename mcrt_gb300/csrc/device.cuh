@@ -8,8 +8,18 @@
 
 #include "layout.h"
 
+// MCRT_NODE_V8: fetch a 64-B BVH node with two 256-bit loads (1) or four 128-bit loads (0).
 #ifndef MCRT_NODE_V8
 #define MCRT_NODE_V8 1
+#endif
+
+// MCRT_COLD: functions of materials the benchmark scenes do not use (Phong, consistent
+// normals) are compiled out of line, which keeps them out of the shading kernel's
+// instruction stream (that kernel misses in the instruction cache; 25.3 -> 25.1 ms per
+// cfg1 frame).  Out-of-line copies of the hot BSDF and environment functions were
+// measured slower: the calls spill more than the smaller code saves.
+#ifndef MCRT_COLD
+#define MCRT_COLD __noinline__
 #endif
 
 namespace mcrt {
@@ -198,8 +208,8 @@ struct TraceCount
 };
 
 // Two-child traversal over FastNode with a per-thread stack in shared memory
-// (`stack` points at this thread's column, entries `stride` ints apart), nearer child
-// first.  FastTrav holds the traversal state; fast_step descends to the next leaf, tests
+// (`stack` points at this thread's column, entries `stride` ints apart): closest-hit
+// queries take the nearer child first, any-hit queries the farther one.  FastTrav holds the traversal state; fast_step descends to the next leaf, tests
 // its triangles and pops.  Measured alternatives on this GPU (cfg1 frame, closest-hit
 // traversal time): postponing leaves until the whole warp holds one (Aila & Laine 2009)
 // 178 vs 132 ms; persistent lanes that take a new ray from the queue when 1-16 lanes of
@@ -267,7 +277,12 @@ __device__ __forceinline__ bool fast_step(FastTrav& r, const FastNode* nodes, co
             if (h0 && h1)
             {
                 int far = n3.y;
-                if (t1n < t0n)
+                // closest hit: nearer child first (cfg1 frame, extension rays: 50.4 ms;
+                // farther first 80.3; nearer exit first 50.4).  Any hit: farther child first
+                // -- a next-event ray leaves the surface it starts on, so an occluder, if there
+                // is one, lies away from the origin (next-event rays: nearer first 57.1 ms,
+                // fixed left-first 46.5, farther first 39.6)
+                if (any ? t1n > t0n : t1n < t0n)
                 {
                     near = n3.y;
                     far = n3.x;
@@ -536,7 +551,7 @@ constexpr int MAT_LGHT = 0, MAT_DIFF = 1, MAT_SPEC = 2, MAT_REFR = 3, MAT_GLSY =
 // 2010): from the interpolated normal np and the interpolated vertex alpha, the normal
 // about which wi reflects to a direction that stays above the surface.  Float operations
 // in the reference's order, no contraction.
-__device__ __forceinline__ float3 consistent_normal(const SceneView& s, int prim, float u, float v, float3 wi,
+__device__ MCRT_COLD float3 consistent_normal(const SceneView& s, int prim, float u, float v, float3 wi,
                                                     float3 np)
 {
     const float4 al = __ldg(&s.prim_alpha[prim]);
@@ -630,6 +645,42 @@ struct BsdfSample
     float  pdf;
 };
 
+// GlossyBSDF (bsdf.cpp:209-301): Phong lobe of exponent 25 about the mirror direction.
+__device__ MCRT_COLD BsdfSample phong_sample(float3 color, float3 wi, float3 nl, float r1, float r2)
+{
+    BsdfSample  s;
+    const float g = 25.f;
+    float       x = r1 * (2.f * kPi);
+    float       r2p = powf(r2, 1.0f / (g + 1.0f));
+    float       st = sqrtf(1.0f - r2p * r2p);
+    float3      c = mk(sinf(x) * st, cosf(x) * st, r2p);
+    float3      refl = reflect_world(wi, nl);
+    Frame       onb(refl);
+    float3      wo = onb.to_world(c);
+    if (dot3(wo, nl) < 0.f) wo = mk(0.f, 0.f, 0.f);
+    float c_o = fmax_ref(dot3(wo, nl), kEpsCos);
+    s.pdf = (g + 1.f) / (2.f * kPi) * powf(fmax_ref(dot3(refl, wo), kEpsCos), g);
+    float w = (g + 2.f) / (g + 1.f) * c_o / fmax_ref(fabsf(dot3(wi, nl)), fabsf(dot3(wo, nl)));
+    if (w != w) w = 0.f;
+    s.weight = color * w;
+    s.wo = wo;
+    return s;
+}
+
+__device__ MCRT_COLD float phong_pdf(float3 wi, float3 nl, float3 wo)
+{
+    float3 refl = reflect_world(wi, nl);
+    return 26.f / (2.f * kPi) * powf(fmax_ref(dot3(refl, wo), kEpsCos), 25.f);
+}
+
+__device__ MCRT_COLD float3 phong_eval(float3 color, float3 wi, float3 nl, float3 wo)
+{
+    float3 refl = reflect_world(wi, nl);
+    float  v = 27.f / (2.f * kPi) * powf(fmax_ref(dot3(refl, wo), kEpsCos), 25.f) /
+              fmax_ref(fabsf(dot3(wi, nl)), fabsf(dot3(wo, nl)));
+    return color * v;
+}
+
 // Material::sample (bsdf.cpp Lambert :51-87, Specular :134-162, Glossy :209-262,
 // Refractive :319-418) plus the GGX conductor (Heitz 2018 visible normals)
 __device__ __forceinline__ BsdfSample bsdf_sample(const Mat& m, float3 wi, float3 nl, float r1, float r2)
@@ -679,21 +730,7 @@ __device__ __forceinline__ BsdfSample bsdf_sample(const Mat& m, float3 wi, float
     }
     else if (m.type == MAT_GLSY)
     {
-        const float g = 25.f;
-        float       x = r1 * (2.f * kPi);
-        float       r2p = powf(r2, 1.0f / (g + 1.0f));
-        float       st = sqrtf(1.0f - r2p * r2p);
-        float3      c = mk(sinf(x) * st, cosf(x) * st, r2p);
-        float3      refl = reflect_world(wi, nl);
-        Frame       onb(refl);
-        float3      wo = onb.to_world(c);
-        if (dot3(wo, nl) < 0.f) wo = mk(0.f, 0.f, 0.f);
-        float c_o = fmax_ref(dot3(wo, nl), kEpsCos);
-        s.pdf = (g + 1.f) / (2.f * kPi) * powf(fmax_ref(dot3(refl, wo), kEpsCos), g);
-        float w = (g + 2.f) / (g + 1.f) * c_o / fmax_ref(fabsf(dot3(wi, nl)), fabsf(dot3(wo, nl)));
-        if (w != w) w = 0.f;
-        s.weight = m.color * w;
-        s.wo = wo;
+        s = phong_sample(m.color, wi, nl, r1, r2);
     }
     else if (m.type == MAT_GGX)
     {
@@ -746,11 +783,7 @@ __device__ __forceinline__ BsdfSample bsdf_sample(const Mat& m, float3 wi, float
 __device__ __forceinline__ float bsdf_pdf(const Mat& m, float3 wi, float3 nl, float3 wo)
 {
     if (m.type == MAT_DIFF) return fmax_ref(dot3(wo, nl), kEpsCos) / kPi;
-    if (m.type == MAT_GLSY)
-    {
-        float3 refl = reflect_world(wi, nl);
-        return 26.f / (2.f * kPi) * powf(fmax_ref(dot3(refl, wo), kEpsCos), 25.f);
-    }
+    if (m.type == MAT_GLSY) return phong_pdf(wi, nl, wo);
     if (m.type == MAT_GGX)
     {
         float3 n = dot3(wi, nl) < 0.f ? -nl : nl;
@@ -767,13 +800,7 @@ __device__ __forceinline__ float bsdf_pdf(const Mat& m, float3 wi, float3 nl, fl
 __device__ __forceinline__ float3 bsdf_eval(const Mat& m, float3 wi, float3 nl, float3 wo)
 {
     if (m.type == MAT_DIFF) return m.color * (1.0f / kPi);
-    if (m.type == MAT_GLSY)
-    {
-        float3 refl = reflect_world(wi, nl);
-        float  v = 27.f / (2.f * kPi) * powf(fmax_ref(dot3(refl, wo), kEpsCos), 25.f) /
-                  fmax_ref(fabsf(dot3(wi, nl)), fabsf(dot3(wo, nl)));
-        return m.color * v;
-    }
+    if (m.type == MAT_GLSY) return phong_eval(m.color, wi, nl, wo);
     if (m.type == MAT_GGX)
     {
         float3 n = dot3(wi, nl) < 0.f ? -nl : nl;
@@ -831,27 +858,25 @@ __device__ __forceinline__ float env_pdf_at(const SceneView& s, int ui, int vi)
     return s.env_norm * lum * static_cast<float>(s.env_w) * static_cast<float>(s.env_h) / (2.f * kPi * kPi);
 }
 
-__device__ __forceinline__ void env_texel(const SceneView& s, float3 d, int& ui, int& vi)
+__device__ __forceinline__ int2 env_texel(int env_w, int env_h, float3 d)
 {
     float phi = acosf(d.y);
     float theta = atanf(d.z / d.x) + kPi * 0.5f;
     if (d.x < 0.f) theta += kPi;
-    ui = clampi(static_cast<int>(theta / (kPi * 2.f) * static_cast<float>(s.env_w)), 0, s.env_w - 1);
-    vi = clampi(static_cast<int>(phi / kPi * static_cast<float>(s.env_h)), 0, s.env_h - 1);
+    return make_int2(clampi(static_cast<int>(theta / (kPi * 2.f) * static_cast<float>(env_w)), 0, env_w - 1),
+                     clampi(static_cast<int>(phi / kPi * static_cast<float>(env_h)), 0, env_h - 1));
 }
 
 __device__ __forceinline__ float env_pdf(const SceneView& s, float3 d)
 {
-    int ui, vi;
-    env_texel(s, d, ui, vi);
-    return env_pdf_at(s, ui, vi);
+    const int2 t = env_texel(s.env_w, s.env_h, d);
+    return env_pdf_at(s, t.x, t.y);
 }
 
 __device__ __forceinline__ float3 env_radiance(const SceneView& s, float3 d)
 {
-    int ui, vi;
-    env_texel(s, d, ui, vi);
-    return xyz(__ldg(&s.env_rgb[ui + vi * s.env_w]));
+    const int2 t = env_texel(s.env_w, s.env_h, d);
+    return xyz(__ldg(&s.env_rgb[t.x + t.y * s.env_w]));
 }
 
 // EnvmapLoader::sample with the two texel-jitter numbers explicit
