@@ -209,7 +209,7 @@ struct TraceCount
 
 // Two-child traversal over FastNode with a per-thread stack in shared memory
 // (`stack` points at this thread's column, entries `stride` ints apart): closest-hit
-// queries take the nearer child first, any-hit queries the farther one.  FastTrav holds the traversal state; fast_step descends to the next leaf, tests
+// queries take the nearer child first, any-hit queries the one left last.  FastTrav holds the traversal state; fast_step descends to the next leaf, tests
 // its triangles and pops.  Measured alternatives on this GPU (cfg1 frame, closest-hit
 // traversal time): postponing leaves until the whole warp holds one (Aila & Laine 2009)
 // 178 vs 132 ms; persistent lanes that take a new ray from the queue when 1-16 lanes of
@@ -278,11 +278,12 @@ __device__ __forceinline__ bool fast_step(FastTrav& r, const FastNode* nodes, co
             {
                 int far = n3.y;
                 // closest hit: nearer child first (cfg1 frame, extension rays: 50.4 ms;
-                // farther first 80.3; nearer exit first 50.4).  Any hit: farther child first
-                // -- a next-event ray leaves the surface it starts on, so an occluder, if there
-                // is one, lies away from the origin (next-event rays: nearer first 57.1 ms,
-                // fixed left-first 46.5, farther first 39.6)
-                if (any ? t1n > t0n : t1n < t0n)
+                // farther first 80.3; nearer exit first 50.4).  Any hit: the child whose box
+                // the ray leaves last first -- a next-event ray leaves the surface it starts
+                // on, so an occluder, if there is one, lies away from the origin (next-event
+                // rays: nearer first 57.1 ms, fixed left-first 46.5, farther entry first 39.7,
+                // farther exit first 39.5, longer overlap first 48.8)
+                if (any ? t1f > t0f : t1n < t0n)
                 {
                     near = n3.y;
                     far = n3.x;
