@@ -105,7 +105,7 @@ class ClockSampler:
 # DRAM bytes per average launch of the traversal kernels on the default cfg1 frame
 # (ncu dram__bytes_read.sum + dram__bytes_write.sum over every launch of three frames,
 # warm caches; profiles/cfg1_dram_traffic.md).  Valid only for that exact configuration.
-CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 508.8e6, "k_extend": 407.2e6}
+CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 594.6e6, "k_extend": 472.7e6}
 
 
 def measured_peak_hbm():
@@ -305,7 +305,8 @@ def main():
     ap.add_argument("--path-chunk", type=int, default=0, help="path slots in flight (0: library default)")
     ap.add_argument("--variant", type=int, default=0, help="traversal kernel variant bits (0: default policy)")
     ap.add_argument("--autotune", action="store_true", help="pick path_chunk / variant with mcrt_autotune first")
-    ap.add_argument("--leaf-size", type=int, default=4, help="BVH leaf size of the scene build (1..15)")
+    ap.add_argument("--leaf-size", type=int, default=0,
+                    help="largest BVH leaf of the scene build (1..15; 0: the library default, 2)")
     args = ap.parse_args()
     args.schedule_id = 0 if args.schedule == "stream" else 1
     if args.impl == "reference":
@@ -417,7 +418,7 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     other = [k for k in kernels if k != dom][0]
     default_cfg1 = (args.workload == "cfg1" and not args.res and not args.spp and not args.path_chunk
-                    and not args.variant and args.traverse == "fast" and args.leaf_size == 4
+                    and not args.variant and args.traverse == "fast" and args.leaf_size in (0, 2)
                     and args.schedule == "stream" and not args.autotune)
     traffic = CFG1_DRAM_BYTES_PER_LAUNCH.get(dom.split()[0]) if default_cfg1 else None
     ob, oms = kernels[other][0], kernels[other][1]
@@ -455,7 +456,7 @@ def main():
             "config": {"workload": text, "traversal": args.traverse, "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"replicas x{world}", "schedule": args.schedule,
                        "path_slots": args.path_chunk or "default", "variant": args.variant,
-                       "leaf_size": args.leaf_size,
+                       "leaf_size": args.leaf_size or 2,
                        "autotuned": tune is not None,
                        "waves_or_iterations_per_step": st_last["waves"],
                        "scene_setup_s": round(setup_s, 2), "scene_device_bytes": sc.info()["device_bytes"], "fast_nodes": sc.info()["fast_nodes"]},

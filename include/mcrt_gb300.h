@@ -94,7 +94,7 @@ typedef struct mcrt_scene_desc {
     int32_t              env_height;
     const float*         env_rgb; /* [env_height][env_width][3], row-major, top row first (envmap.h:20-25) */
     int32_t              builder; /* MCRT_BUILD_* */
-    int32_t              leaf_size; /* own builder: max triangles per leaf (0 -> 4) */
+    int32_t              leaf_size; /* own builder: max triangles per leaf (0 -> 2) */
     const mcrt_bvh_tree* external_tree;
     /* [num_triangles][3] per-corner alpha for MCRT_MAT_CONSISTENT materials
      * (TriangleObject::m_vertex_alpha as Mesh::genNormals computes it, mesh.cpp:92-115);
@@ -212,7 +212,7 @@ int mcrt_vertex_alpha(const float* vertices, const float* normals, int64_t num_t
  * no GPU needed), returned in the mcrt_bvh_tree form of the reference SplitBVH dump.  Call
  * with node_box == NULL to get *num_nodes / *num_refs, then with arrays of those sizes
  * (node_box [6 * nodes], node_info [6 * nodes], ref_prim [refs], ref_box [6 * refs]).
- * leaf_size: max references per leaf (1..15, 0 -> 4).  Replaces SplitBVH::SplitBVH
+ * leaf_size: max references per leaf (1..15, 0 -> 2).  Replaces SplitBVH::SplitBVH
  * (splitbvh.cpp:1410-1625) for callers that build trees themselves. */
 int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int32_t leaf_size, int32_t* num_nodes,
                    int32_t* num_refs, float* node_box, int32_t* node_info, int32_t* ref_prim, float* ref_box);

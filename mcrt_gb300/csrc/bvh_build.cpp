@@ -193,7 +193,7 @@ struct Builder
 
 void build_sah_tree(const float* v, int64_t n, int leaf_size, BinaryTree& out)
 {
-    if (leaf_size <= 0) leaf_size = 4;
+    if (leaf_size <= 0) leaf_size = kDefaultLeafSize;
     std::vector<Box>     boxes(n);
     std::vector<float>   cen(3 * n);
     std::vector<int32_t> prims(n);

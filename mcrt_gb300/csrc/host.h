@@ -20,6 +20,11 @@ struct BinaryTree
     int                  root = 0;
 };
 
+// Default largest leaf of the library's builder.  Per cfg1 frame (1.3 M triangles), ms:
+// leaves of <= 2 triangles 118.3, <= 3 118.7, <= 4 120.5, <= 6 126.1, <= 8 131.3 -- a
+// watertight triangle test costs more than a two-box node step.
+constexpr int kDefaultLeafSize = 2;
+
 // Binned-SAH object-split builder (own design; leaf <= leaf_size references).
 // Multithreaded over subtrees.  Leaves reference contiguous runs of ref_prim.
 void build_sah_tree(const float* vertices, int64_t num_tris, int leaf_size, BinaryTree& out);

@@ -207,7 +207,7 @@ uint64_t scene_desc_hash(const mcrt_scene_desc& d)
     h.add_value(has_alpha);
     if (d.vertex_alpha) h.add(d.vertex_alpha, sizeof(float) * 3 * static_cast<size_t>(d.num_triangles));
     h.add_value(d.builder);
-    const int32_t leaf = d.leaf_size > 0 ? d.leaf_size : 4;
+    const int32_t leaf = d.leaf_size > 0 ? d.leaf_size : kDefaultLeafSize;
     h.add_value(leaf);
     if (d.builder == MCRT_BUILD_EXTERNAL && d.external_tree)
     {
@@ -364,7 +364,7 @@ extern "C" int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int3
     try
     {
         BinaryTree t;
-        build_sah_tree(vertices, num_triangles, leaf_size > 0 ? leaf_size : 4, t);
+        build_sah_tree(vertices, num_triangles, leaf_size > 0 ? leaf_size : kDefaultLeafSize, t);
         const int64_t nodes = static_cast<int64_t>(t.node_info.size() / 6);
         const int64_t refs = static_cast<int64_t>(t.ref_prim.size());
         if (nodes > INT32_MAX || refs > INT32_MAX) return set_error(MCRT_ERR_INVALID_ARGUMENT, "tree too large");

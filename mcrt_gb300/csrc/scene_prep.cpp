@@ -179,7 +179,7 @@ std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs)
     }
     else if (d.builder == MCRT_BUILD_SAH)
     {
-        int leaf = d.leaf_size > 0 ? d.leaf_size : 4;
+        int leaf = d.leaf_size > 0 ? d.leaf_size : kDefaultLeafSize;
         if (leaf > 15) return "leaf_size must be <= 15";
         build_sah_tree(d.vertices, n, leaf, tree);
     }

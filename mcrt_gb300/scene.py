@@ -109,7 +109,7 @@ def _stream_ptr():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def _c_desc(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = None, leaf_size: int = 4):
+def _c_desc(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = None, leaf_size: int = 0):
     """The C description of a scene and the arrays it points into (keep them alive)."""
     v = np.ascontiguousarray(desc.vertices, np.float32).reshape(-1, 9)
     mid = np.ascontiguousarray(desc.material_ids, np.int32)
@@ -155,7 +155,7 @@ def vertex_alpha(vertices, normals) -> np.ndarray:
     return out
 
 
-def build_bvh(vertices, leaf_size: int = 4) -> dict:
+def build_bvh(vertices, leaf_size: int = 0) -> dict:
     """mcrt_build_bvh: the library's binned-SAH tree of (n, 9) triangle vertices, in the
     form of a reference SplitBVH dump (node_box, node_info, ref_prim, ref_box; root 0)."""
     lib = N.load()
@@ -184,7 +184,7 @@ def sah_cost(tree: dict, c_node: float = 1.0, c_tri: float = 1.0, root: int = 0)
     return float((c_node * area[~leaf].sum() + c_tri * (area[leaf] * ni[leaf, 5]).sum()) / area[root])
 
 
-def desc_hash(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = None, leaf_size: int = 4) -> int:
+def desc_hash(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = None, leaf_size: int = 0) -> int:
     """mcrt_scene_desc_hash: the key a scene cache file is written under."""
     d, keep = _c_desc(desc, builder, external_tree, leaf_size)
     h = ctypes.c_uint64()
@@ -197,7 +197,7 @@ class GpuScene:
     """A finalized scene on the GPU (owns its device memory)."""
 
     def __init__(self, desc: SceneDesc, builder: str = "sah", external_tree: dict | None = None,
-                 leaf_size: int = 4):
+                 leaf_size: int = 0):
         lib = N.load()
         self._lib = lib
         self.desc = desc
