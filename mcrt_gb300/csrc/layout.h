@@ -71,7 +71,7 @@ struct __align__(16) LightGPU
 // Read-only view of one uploaded scene (device pointers).
 // guide-table resolution of the environment-map CDF searches (powers of two)
 constexpr int kEnvGuideM = 256;
-constexpr int kEnvGuideC = 64;
+constexpr int kEnvGuideC = 256;  // 64: 0.3 ms more shading per cfg1 frame
 
 struct SceneView
 {

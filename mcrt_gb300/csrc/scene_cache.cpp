@@ -25,7 +25,7 @@
 namespace mcrt {
 namespace {
 
-constexpr uint32_t kFormat = 2;
+constexpr uint32_t kFormat = 3;
 constexpr int      kArrays = 15;
 const char         kMagic[8] = {'M', 'C', 'R', 'T', 'S', 'C', 'N', '\0'};
 
