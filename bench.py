@@ -332,6 +332,7 @@ def main():
     import mcrt_gb300
     from mcrt_gb300 import GpuScene, TRAVERSE_FAST, TRAVERSE_REF
     from mcrt_gb300._native import PROFILE_COUNT, PROFILE_STAGES
+    from mcrt_gb300.replicas import aggregate
 
     mcrt_gb300.load()
     desc, cam, p, text = workload(args.workload)
@@ -385,13 +386,7 @@ def main():
             st_last = st
     clocks = clk.summary()
     total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-        r = torch.tensor([float(rays), float(paths)], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(r)
-        rays, paths = int(r[0].item()), int(r[1].item())
+    total_ms, rays, paths = aggregate(total_ms, rays, paths, dev)
     value = rays / (total_ms / 1e3) / 1e6
     msamples = paths / (total_ms / 1e3) / 1e6
 
