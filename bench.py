@@ -105,7 +105,7 @@ class ClockSampler:
 # DRAM bytes per average launch of the traversal kernels on the default cfg1 frame
 # (ncu dram__bytes_read.sum + dram__bytes_write.sum over every launch of three frames,
 # warm caches; profiles/cfg1_dram_traffic.md).  Valid only for that exact configuration.
-CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 594.6e6, "k_extend": 472.7e6}
+CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 594.9e6, "k_extend": 473.1e6}
 
 
 def measured_peak_hbm():
@@ -115,6 +115,22 @@ def measured_peak_hbm():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+def l2_read_peak():
+    """L2 read bandwidth of this GPU, measured live by the library's probe kernel
+    (mcrt_probe_l2_read: a 48 MB L2-resident buffer read 100 times in one launch), best of 3.
+    The traversal kernels' node and triangle reads mostly hit L2, so their algorithmic
+    bandwidth is also quoted against this figure."""
+    import ctypes
+    from mcrt_gb300 import _native as N
+    lib = N.load()
+    best = 0.0
+    for _ in range(3):
+        g = ctypes.c_float(0.0)
+        N.check(lib.mcrt_probe_l2_read(48 << 20, 100, ctypes.byref(g), None), "mcrt_probe_l2_read")
+        best = max(best, g.value)
+    return best
 
 
 def cpu_port_sample(desc, cam, p, rows, seed=7, osc=None):
@@ -411,6 +427,7 @@ def main():
     avg_launch_ms = kern_ms / max(extend_launches, 1)
     achieved = per_launch_bytes / (avg_launch_ms / 1e3) / 1e9 if avg_launch_ms > 0 else 0.0
     peak, peak_kind = measured_peak_hbm()
+    l2_peak = l2_read_peak()
     other = [k for k in kernels if k != dom][0]
     default_cfg1 = (args.workload == "cfg1" and not args.res and not args.spp and not args.path_chunk
                     and not args.variant and args.traverse == "fast" and args.leaf_size in (0, 2)
@@ -463,12 +480,16 @@ def main():
                          "traffic_unit": "bytes per launch (ncu DRAM read + write, warm caches)",
                          "algorithmic_bytes_per_launch": int(per_launch_bytes),
                          "peak_source": peak_kind,
+                         "l2": {"peak": round(l2_peak, 1), "unit": "GB/s",
+                                "frac": round(achieved / l2_peak, 4) if l2_peak > 0 else None,
+                                "how": "mcrt_probe_l2_read: 48 MB L2-resident buffer read 100 times per launch, best of 3, in this run"},
                          "bytes_per_ray": round(bytes_per_render / max(kern_rays, 1), 1),
                          "nodes_per_ray": round(kern_nodes / max(kern_rays, 1), 2),
                          "tris_per_ray": round(kern_tris / max(kern_rays, 1), 2),
                          "share_of_step": round(kern_ms / max(total_ms, 1e-9), 3),
                          "second_kernel": {"kernel": other, "achieved": round(other_achieved, 1),
                                            "frac": round(other_achieved / peak, 4),
+                                           "frac_l2": round(other_achieved / l2_peak, 4) if l2_peak > 0 else None,
                                            "share_of_step": round(oms / max(total_ms, 1e-9), 3)}},
             "stage_ms_per_step": {"begin+regen": round(st_last["stage_ms"][0], 2),
                                   "extend": round(st_last["stage_ms"][1], 2), "shade": round(st_last["stage_ms"][2], 2),

@@ -324,6 +324,12 @@ int mcrt_autotune(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_camera
 int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera, const mcrt_render_params* params,
                         float* rgb_out_device, mcrt_render_stats* stats, void* stream);
 
+/* L2 read bandwidth of the current GPU in GB/s (no reference counterpart: a roofline
+ * denominator for the traversal kernels, whose node and triangle reads mostly hit L2).
+ * Reads an L2-resident buffer of `bytes` (1 MB .. 96 MB) `reps` times (1 .. 1000) in one
+ * launch with L1-bypassing 16-B loads; allocates and frees its buffer; blocks. */
+int mcrt_probe_l2_read(int64_t bytes, int32_t reps, float* gbs, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

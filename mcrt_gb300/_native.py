@@ -127,6 +127,7 @@ EXPORTS = {
     "mcrt_film_encode": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int64, ctypes.POINTER(c_int64),
                                    c_int32, c_void_p]),
     "mcrt_film_tonemap": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_float, c_int32, c_void_p]),
+    "mcrt_probe_l2_read": (c_int32, [c_int64, c_int32, ctypes.POINTER(c_float), c_void_p]),
     "mcrt_autotune": (c_int32, [c_int32, ctypes.POINTER(c_void_p), ctypes.POINTER(Camera),
                                 ctypes.POINTER(RenderParams), ctypes.POINTER(RenderParams),
                                 ctypes.POINTER(TuneReport), c_void_p]),
