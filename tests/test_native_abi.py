@@ -36,6 +36,9 @@ def test_null_arguments_fail_cleanly(native):
     rc = native.mcrt_trace_closest(None, None, 0, None, 0, 0, None)
     assert rc == -1
     assert native.mcrt_scene_destroy(None) == 0
+    g = ctypes.c_float(0.0)
+    assert native.mcrt_probe_l2_read(0, 10, ctypes.byref(g), None) == -1  # sizes checked before any device work
+    assert native.mcrt_probe_l2_read(48 << 20, 0, ctypes.byref(g), None) == -1
 
 
 def test_scene_desc_validation_before_any_device_work(native):

@@ -124,3 +124,14 @@ def test_empty_and_single_ray(cuda_device):
     for mode in (TRAVERSE_FAST, TRAVERSE_REF):
         out = sc.trace_closest(r, mode)
         assert out[0, 3].view(np.int32) == fx["prim_primary"][0]
+
+
+def test_l2_read_probe(cuda_device):
+    """The L2 roofline denominator: a plausible bandwidth, above the HBM copy rate of this
+    class of GPU (several TB/s) and below any L2's (100 TB/s)."""
+    import ctypes
+    from mcrt_gb300 import _native as N
+    lib = N.load()
+    g = ctypes.c_float(0.0)
+    N.check(lib.mcrt_probe_l2_read(48 << 20, 20, ctypes.byref(g), None), "mcrt_probe_l2_read")
+    assert 3000.0 < g.value < 100000.0, g.value
