@@ -23,6 +23,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -54,7 +55,10 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples go to MCRT_CLOCKS_DIR (default: the temp directory); the JSON line
+        # carries their summary
+        self.path = os.path.join(os.environ.get("MCRT_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"mcrt_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
