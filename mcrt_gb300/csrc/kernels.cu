@@ -140,8 +140,7 @@ __global__ void k_render_begin(WaveArgs a, int waves, int64_t limit)
     c->scount[0] = c->scount[1] = 0;
     c->new_base = c->new_count = 0;
     c->chunk = -1;
-    c->fetch[0] = c->fetch[1] = 0;
-    c->pad = 0;
+    c->fetch[0] = c->fetch[1] = c->fetch[2] = 0;
     c->next = 0;
     c->limit = waves ? 0ull : static_cast<unsigned long long>(limit);
     c->new_g = 0;
@@ -165,6 +164,7 @@ __global__ void k_iter_begin(WaveArgs a, int p)
     c->scount[1] = 0;
     c->fetch[0] = 0;
     c->fetch[1] = 0;
+    c->fetch[2] = 0;
     // top the queue up with new paths (continuing rays are already in it)
     const int                q = c->qcount[p];
     const unsigned long long avail = c->limit > c->next ? c->limit - c->next : 0ull;
@@ -682,11 +682,9 @@ __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
 // Adjoint (ADJ): the emission derivative of each next-event contribution (the
 // coefficient of the reached emitter's E)
 template <bool ADJ>
-__device__ __forceinline__ void connect_result(const WaveArgs& a, const Grads& G, int p, int n0, int i, bool hit,
+__device__ __forceinline__ void connect_result(const WaveArgs& a, const Grads& G, int p, int q, int k, bool hit,
                                                const Hit& h)
 {
-    const int        q = i < n0 ? 0 : 1;
-    const int        k = i < n0 ? i : i - n0;
     const float4     d = a.sd[q][k], v = a.sv[q][k];
     const int4       m = a.sm[q][k];
     const JobGPU&    J = a.jobs[m.w];
@@ -702,31 +700,32 @@ __device__ __forceinline__ void connect_result(const WaveArgs& a, const Grads& G
     }
 }
 
-template <int STACK, bool COUNT, int MINB, bool ADJ>
-__global__ void __launch_bounds__(kTraceBlock, MINB) k_connect(WaveArgs a, int p)
+// Q = 0: the any-hit queue (rays to the environment); Q = 1: the bounded closest-hit
+// queue (rays to area lights).  One kernel per queue: the any-hit build needs no
+// closest-hit state, so it fits 56 registers without spills (both in one kernel spilled
+// 80 B; next-event stage 37.8 -> 37.5 ms per cfg1 frame) and runs capped at 48 registers
+// for 10 blocks per SM (kAnyHitMinBlocks; 36.5 ms).
+template <int STACK, bool COUNT, int MINB, bool ADJ, int Q>
+__global__ void __launch_bounds__(kTraceBlock, (Q == 0 && MINB > 1) ? kAnyHitMinBlocks : MINB)
+    k_connect(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];
     __shared__ int stack[STACK * kTraceBlock];
     const Grads    G = grads_begin<ADJ>(a, sgrad);
     int*           st = stack + threadIdx.x;
     TraceCount     cnt = {0u, 0u};
-    const int      n0 = min(a.ctrl->scount[0], static_cast<int>(a.shadow_cap));
-    const int      n1 = min(a.ctrl->scount[1], static_cast<int>(a.shadow_cap));
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats[1], static_cast<unsigned long long>(n0 + n1));
-    for (QueueWalk w(&a.ctrl->fetch[1], n0 + n1, a.batch_fetch != 0); w.valid(); w.next())
+    const int      n = min(a.ctrl->scount[Q], static_cast<int>(a.shadow_cap));
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(&a.stats[1], static_cast<unsigned long long>(n));
+    for (QueueWalk w(&a.ctrl->fetch[1 + Q], n, a.batch_fetch != 0); w.valid(); w.next())
     {
-        const int i = w.i;
-        if (i >= n0 + n1) continue;
-        int           q = i < n0 ? 0 : 1;
-        int           k = i < n0 ? i : i - n0;
-        float4        o = a.so[q][k], d = a.sd[q][k];
-        const JobGPU& J = a.jobs[a.sm[q][k].w];
+        const int k = w.i;
+        if (k >= n) continue;
+        float4        o = a.so[Q][k], d = a.sd[Q][k];
+        const JobGPU& J = a.jobs[a.sm[Q][k].w];
         Hit           h;
-        bool hit = q == 0 ? trace_ray<true, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock,
-                                                          h, a.err, &cnt)
-                          : trace_ray<false, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st,
-                                                           kTraceBlock, h, a.err, &cnt);
-        connect_result<ADJ>(a, G, p, n0, i, hit, h);
+        bool hit = trace_ray<Q == 0, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock, h,
+                                                   a.err, &cnt);
+        connect_result<ADJ>(a, G, p, Q, k, hit, h);
     }
     if (COUNT) flush_count(a.stats, 4, cnt);
     grads_end<ADJ>(a, sgrad);
@@ -1141,7 +1140,7 @@ struct StageTimer
     }
 };
 
-// one iteration of parity p (five launches); stage timer slots: 0 begin + regen,
+// one iteration of parity p (six launches); stage timer slots: 0 begin + regen,
 // 1 extend, 2 shade, 3 connect
 template <int STACK, bool COUNT, int MINB, bool ADJ = false>
 void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, StageTimer* tm, size_t dyn = 0)
@@ -1163,7 +1162,8 @@ void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t 
     k_shade<ADJ><<<ls.grid_shade, 128, dyn, st>>>(a, p);
     end();
     beg(3);
-    k_connect<STACK, COUNT, MINB, ADJ><<<ls.grid_connect, kTraceBlock, dyn, st>>>(a, p);
+    k_connect<STACK, COUNT, MINB, ADJ, 0><<<ls.grid_any, kTraceBlock, dyn, st>>>(a, p);
+    k_connect<STACK, COUNT, MINB, ADJ, 1><<<ls.grid_connect, kTraceBlock, dyn, st>>>(a, p);
     end();
 }
 
@@ -1326,7 +1326,7 @@ int run_waves(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<i
     run.table_bytes = 8 * static_cast<int64_t>(table.size());
     const int iters = wave_iterations(max_depth);
     run.waves = num_chunks;
-    run.launches = 1 + num_chunks * (1 + 5 * iters);
+    run.launches = 1 + num_chunks * (1 + 6 * iters);
     run.extend_launches = num_chunks * iters;
     auto enqueue = [&](cudaStream_t s2, StageTimer* tm) {
         with_variant(stack32, regcap, count, WaveEnqueue{&a, max_depth, &lsv, s2, tm});
@@ -1443,7 +1443,7 @@ int stream_loop(Workspace& w, const WaveArgs& a, int64_t total, int max_depth, b
     release_graph();
     if (e != cudaSuccess) return fail(MCRT_ERR_CUDA, std::string("streaming render: ") + cudaGetErrorString(e));
     run.waves = iters;
-    run.launches += iters * 5;
+    run.launches += iters * 6;
     run.extend_launches = iters;
     return MCRT_OK;
 }
@@ -1483,14 +1483,18 @@ int adjoint_launch_shape(size_t dyn, LaunchShape& ls)
     CK(cudaFuncSetAttribute(k_regen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
     CK(cudaFuncSetAttribute(k_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
     constexpr int B = kTraceMinBlocks;
-    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            static_cast<int>(dyn)));
+    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                             static_cast<int>(dyn)));
     const int sms = num_sms();
-    int       occ_e = 0, occ_s = 0, occ_c = 0;
+    int       occ_e = 0, occ_s = 0, occ_a = 0, occ_c = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_extend<STACK, false, B>, kTraceBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<true>, 128, dyn);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_connect<STACK, false, B, true>, kTraceBlock, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_connect<STACK, false, B, true, 0>, kTraceBlock, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_connect<STACK, false, B, true, 1>, kTraceBlock, dyn);
     ls.grid_trace = sms * std::max(occ_e, 1);
+    ls.grid_any = sms * std::max(occ_a, 1);
     ls.grid_connect = sms * std::max(occ_c, 1);
     ls.grid_shade = sms * std::max(occ_s, 1);
     ls.grid_small = sms * 8;
@@ -1744,16 +1748,26 @@ LaunchShape launch_shape_variant(bool stack32, bool regcap)
 {
     LaunchShape ls;
     int         sms = num_sms();
-    int         occ_t = 0, occ_s = 0;
+    int         occ_t = 0, occ_s = 0, occ_a = 0;
     constexpr int B = kTraceMinBlocks;
     if (stack32)
+    {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, regcap ? k_extend<32, false, B> : k_extend<32, false, 1>,
                                                       kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ_a, regcap ? k_connect<32, false, B, false, 0> : k_connect<32, false, 1, false, 0>, kTraceBlock, 0);
+    }
     else
+    {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &occ_t, regcap ? k_extend<kStack, false, B> : k_extend<kStack, false, 1>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ_a, regcap ? k_connect<kStack, false, B, false, 0> : k_connect<kStack, false, 1, false, 0>,
+            kTraceBlock, 0);
+    }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<false>, 128, 0);
     ls.grid_trace = sms * std::max(occ_t, 1);
+    ls.grid_any = sms * std::max(occ_a, 1);
     ls.grid_connect = ls.grid_trace;
     ls.grid_shade = sms * std::max(occ_s, 1);
     ls.grid_small = sms * 8;

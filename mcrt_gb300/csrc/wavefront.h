@@ -35,6 +35,10 @@ constexpr int kStack = 64;
 // 8 blocks (64 registers) 52.6 / 59.9 ms extend / connect, 9 blocks 52.2 / 56.7, 10 blocks
 // (48 registers, spills) 54.4 / 57.0.
 constexpr int kTraceMinBlocks = 9;
+// The any-hit next-event kernel under MCRT_VARIANT_REGCAP: 48 registers, 10 blocks per SM.
+// Next-event stage per cfg1 frame: 9 blocks 37.5 ms, 10 blocks 36.5, 12 blocks (40
+// registers, spills) 38.8.
+constexpr int kAnyHitMinBlocks = 10;
 constexpr int kMaxDepth = 62;
 constexpr int64_t kMaxQueue = int64_t(1) << 27;     // rays per queue (result indices stay in int)
 constexpr int64_t kDefaultQueue = int64_t(1) << 24;  // streaming schedule default (12 GB of queues)
@@ -48,8 +52,7 @@ struct Ctrl
     int                new_base;   // this iteration's admitted paths: first queue position
     int                new_count;  //   and how many
     int                chunk;      // wave schedule: index of the current wave
-    int                fetch[2];   // rays taken so far by this iteration's k_extend, k_connect warps
-    int                pad;
+    int                fetch[3];   // rays taken so far by this iteration's k_extend, k_connect<0>, k_connect<1>
     unsigned long long next;      // index of the next path to admit
     unsigned long long limit;     // admission limit (exclusive)
     unsigned long long new_g;     // index of the first path admitted this iteration
@@ -113,7 +116,7 @@ constexpr int kAdjLog = 16;
 
 struct LaunchShape
 {
-    int grid_trace, grid_connect, grid_shade, grid_small, block;
+    int grid_trace, grid_any, grid_connect, grid_shade, grid_small, block;  // grid_any: any-hit k_connect
 };
 
 // sub-array allocator: consecutive 256-B aligned pieces of one block
