@@ -500,11 +500,14 @@ __device__ __forceinline__ void refine_hit(const SceneView& s, float3 o, float3 
     }
 }
 
-template <bool ANY, int STACK, bool COUNT = false>
+// REFM = false: a build for jobs that all traverse in FAST mode; without the reference
+// traversal in the same kernel the fast one needs fewer registers (the any-hit kernel at
+// 48 registers: 8 B of spills instead of 52).
+template <bool ANY, int STACK, bool COUNT = false, bool REFM = true>
 __device__ __forceinline__ bool trace_ray(const SceneView& s, int mode, float3 o, float3 d, float tmin, float tmax,
                                           int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr)
 {
-    if (mode == 1) return trace_ref<ANY, STACK>(s, o, d, tmin, tmax, stack, stride, hit, err);
+    if (REFM && mode == 1) return trace_ref<ANY, STACK>(s, o, d, tmin, tmax, stack, stride, hit, err);
     bool found = trace_fast<ANY, STACK, COUNT>(s, o, d, tmin, tmax, stack, stride, hit, err, cnt);
     if (!ANY && found) refine_hit(s, o, d, tmin, hit);
     return found;

@@ -456,7 +456,7 @@ __device__ __forceinline__ float4 hit_record(bool hit, const Hit& h)
     return hit ? make_float4(h.t, h.u, h.v, __int_as_float(h.prim)) : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
 }
 
-template <int STACK, bool COUNT, int MINB>
+template <int STACK, bool COUNT, int MINB, bool REFM = true>
 __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
 {
     __shared__ int stack[STACK * kTraceBlock];
@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
         float4        o = a.qo[p][i], d = a.qd[p][i];
         const JobGPU& J = a.jobs[__float_as_int(o.w)];
         Hit           h;
-        bool hit = trace_ray<false, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), kEpsRay, inf, st, kTraceBlock, h,
+        bool hit = trace_ray<false, STACK, COUNT, REFM>(J.scene, J.traverse, xyz(o), xyz(d), kEpsRay, inf, st, kTraceBlock, h,
                                                   a.err, &cnt);
         a.hits[i] = hit_record(hit, h);
     }
@@ -705,7 +705,7 @@ __device__ __forceinline__ void connect_result(const WaveArgs& a, const Grads& G
 // closest-hit state, so it fits 56 registers without spills (both in one kernel spilled
 // 80 B; next-event stage 37.8 -> 37.5 ms per cfg1 frame) and runs capped at 48 registers
 // for 10 blocks per SM (kAnyHitMinBlocks; 36.5 ms).
-template <int STACK, bool COUNT, int MINB, bool ADJ, int Q>
+template <int STACK, bool COUNT, int MINB, bool ADJ, int Q, bool REFM = true>
 __global__ void __launch_bounds__(kTraceBlock, (Q == 0 && MINB > 1) ? kAnyHitMinBlocks : MINB)
     k_connect(WaveArgs a, int p)
 {
@@ -723,7 +723,7 @@ __global__ void __launch_bounds__(kTraceBlock, (Q == 0 && MINB > 1) ? kAnyHitMin
         float4        o = a.so[Q][k], d = a.sd[Q][k];
         const JobGPU& J = a.jobs[a.sm[Q][k].w];
         Hit           h;
-        bool hit = trace_ray<Q == 0, STACK, COUNT>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock, h,
+        bool hit = trace_ray<Q == 0, STACK, COUNT, REFM>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock, h,
                                                    a.err, &cnt);
         connect_result<ADJ>(a, G, p, Q, k, hit, h);
     }
@@ -1142,7 +1142,7 @@ struct StageTimer
 
 // one iteration of parity p (six launches); stage timer slots: 0 begin + regen,
 // 1 extend, 2 shade, 3 connect
-template <int STACK, bool COUNT, int MINB, bool ADJ = false>
+template <int STACK, bool COUNT, int MINB, bool ADJ = false, bool REFM = true>
 void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, StageTimer* tm, size_t dyn = 0)
 {
     auto beg = [&](int stg) {
@@ -1156,27 +1156,27 @@ void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t 
     k_regen<ADJ><<<ls.grid_shade, 128, dyn, st>>>(a, p);
     end();
     beg(1);
-    k_extend<STACK, COUNT, MINB><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, p);
+    k_extend<STACK, COUNT, MINB, REFM><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, p);
     end();
     beg(2);
     k_shade<ADJ><<<ls.grid_shade, 128, dyn, st>>>(a, p);
     end();
     beg(3);
-    k_connect<STACK, COUNT, MINB, ADJ, 0><<<ls.grid_any, kTraceBlock, dyn, st>>>(a, p);
-    k_connect<STACK, COUNT, MINB, ADJ, 1><<<ls.grid_connect, kTraceBlock, dyn, st>>>(a, p);
+    k_connect<STACK, COUNT, MINB, ADJ, 0, REFM><<<ls.grid_any, kTraceBlock, dyn, st>>>(a, p);
+    k_connect<STACK, COUNT, MINB, ADJ, 1, REFM><<<ls.grid_connect, kTraceBlock, dyn, st>>>(a, p);
     end();
 }
 
 // one wave of the wave schedule: admit the wave, then iterate until its last path is
 // finished (an even count, so the next wave starts on parity 0)
-template <int STACK, bool COUNT, int MINB>
+template <int STACK, bool COUNT, int MINB, bool REFM = true>
 void enqueue_wave(const WaveArgs& a, int max_depth, const LaunchShape& ls, cudaStream_t st, StageTimer* tm)
 {
     if (tm) tm->record(st, 0, true);
     k_wave_next<<<1, 1, 0, st>>>(a);
     if (tm) tm->record(st, 0, false);
     const int iters = wave_iterations(max_depth);
-    for (int t = 0; t < iters; ++t) enqueue_iter<STACK, COUNT, MINB>(a, t & 1, ls, st, tm);
+    for (int t = 0; t < iters; ++t) enqueue_iter<STACK, COUNT, MINB, false, REFM>(a, t & 1, ls, st, tm);
 }
 
 int validate_job_impl(const mcrt_scene* s, const mcrt_camera* c, const mcrt_render_params* p)
@@ -1215,10 +1215,10 @@ struct WaveEnqueue
     const LaunchShape* ls;
     cudaStream_t       st;
     StageTimer*        tm;
-    template <int S, bool C, int M>
+    template <int S, bool C, int M, bool R>
     void run() const
     {
-        enqueue_wave<S, C, M>(*a, max_depth, *ls, st, tm);
+        enqueue_wave<S, C, M, R>(*a, max_depth, *ls, st, tm);
     }
 };
 
@@ -1229,31 +1229,35 @@ struct IterEnqueue
     const LaunchShape* ls;
     cudaStream_t       st;
     StageTimer*        tm;
-    template <int S, bool C, int M>
+    template <int S, bool C, int M, bool R>
     void run() const
     {
-        enqueue_iter<S, C, M>(*a, p, *ls, st, tm);
+        enqueue_iter<S, C, M, false, R>(*a, p, *ls, st, tm);
     }
 };
 
-// dispatch of the traversal-kernel template variants
+// dispatch of the traversal-kernel template variants.  Jobs that all traverse in FAST
+// mode (f.ls->fast_only) get the builds without the REF traversal; any REF job runs the
+// general build with 64-entry stacks and no register cap.
 template <class F>
 void with_variant(bool stack32, bool regcap, bool count, const F& f)
 {
     constexpr int B = kTraceMinBlocks;
-    if (stack32)
+    if (!f.ls->fast_only)
+        count ? f.template run<kStack, true, 1, true>() : f.template run<kStack, false, 1, true>();
+    else if (stack32)
     {
         if (regcap)
-            count ? f.template run<32, true, B>() : f.template run<32, false, B>();
+            count ? f.template run<32, true, B, false>() : f.template run<32, false, B, false>();
         else
-            count ? f.template run<32, true, 1>() : f.template run<32, false, 1>();
+            count ? f.template run<32, true, 1, false>() : f.template run<32, false, 1, false>();
     }
     else
     {
         if (regcap)
-            count ? f.template run<kStack, true, B>() : f.template run<kStack, false, B>();
+            count ? f.template run<kStack, true, B, false>() : f.template run<kStack, false, B, false>();
         else
-            count ? f.template run<kStack, true, 1>() : f.template run<kStack, false, 1>();
+            count ? f.template run<kStack, true, 1, false>() : f.template run<kStack, false, 1, false>();
     }
 }
 
@@ -1622,7 +1626,9 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     const int   vb = (p0.variant & MCRT_VARIANT_EXPLICIT) ? p0.variant : (MCRT_VARIANT_STACK32 | MCRT_VARIANT_REGCAP);
     const bool  stack32 = (vb & MCRT_VARIANT_STACK32) && bvh_depth + 2 < 32;
     const bool  regcap = (vb & MCRT_VARIANT_REGCAP) != 0;
-    LaunchShape lsv = launch_shape_variant(stack32, regcap);
+    bool        fast_only = true;
+    for (const JobGPU& J : jobs) fast_only = fast_only && J.traverse != MCRT_TRAVERSE_REF;
+    LaunchShape lsv = launch_shape_variant(stack32, regcap, fast_only);
     Workspace&  w = owner->ws;
     w.args.batch_fetch = (vb & MCRT_VARIANT_GRIDSTRIDE) ? 0 : 1;
     StageTimer  timer;
@@ -1744,27 +1750,36 @@ void enqueue_render_begin(const WaveArgs& a, bool waves, int64_t limit, cudaStre
 
 LaunchShape launch_shape() { return launch_shape_variant(false, false); }
 
-LaunchShape launch_shape_variant(bool stack32, bool regcap)
+LaunchShape launch_shape_variant(bool stack32, bool regcap, bool fast_only)
 {
     LaunchShape ls;
     int         sms = num_sms();
     int         occ_t = 0, occ_s = 0, occ_a = 0;
     constexpr int B = kTraceMinBlocks;
-    if (stack32)
+    if (!fast_only)  // the general build (see with_variant)
     {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, regcap ? k_extend<32, false, B> : k_extend<32, false, 1>,
-                                                      kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, k_extend<kStack, false, 1, true>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_connect<kStack, false, 1, false, 0, true>, kTraceBlock,
+                                                      0);
+    }
+    else if (stack32)
+    {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ_a, regcap ? k_connect<32, false, B, false, 0> : k_connect<32, false, 1, false, 0>, kTraceBlock, 0);
+            &occ_t, regcap ? k_extend<32, false, B, false> : k_extend<32, false, 1, false>, kTraceBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &occ_a, regcap ? k_connect<32, false, B, false, 0, false> : k_connect<32, false, 1, false, 0, false>,
+            kTraceBlock, 0);
     }
     else
     {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ_t, regcap ? k_extend<kStack, false, B> : k_extend<kStack, false, 1>, kTraceBlock, 0);
+            &occ_t, regcap ? k_extend<kStack, false, B, false> : k_extend<kStack, false, 1, false>, kTraceBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ_a, regcap ? k_connect<kStack, false, B, false, 0> : k_connect<kStack, false, 1, false, 0>,
+            &occ_a,
+            regcap ? k_connect<kStack, false, B, false, 0, false> : k_connect<kStack, false, 1, false, 0, false>,
             kTraceBlock, 0);
     }
+    ls.fast_only = fast_only;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<false>, 128, 0);
     ls.grid_trace = sms * std::max(occ_t, 1);
     ls.grid_any = sms * std::max(occ_a, 1);

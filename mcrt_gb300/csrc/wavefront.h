@@ -117,6 +117,7 @@ constexpr int kAdjLog = 16;
 struct LaunchShape
 {
     int grid_trace, grid_any, grid_connect, grid_shade, grid_small, block;  // grid_any: any-hit k_connect
+    bool fast_only = false;  // every job traverses in FAST mode: kernels built without the REF traversal
 };
 
 // sub-array allocator: consecutive 256-B aligned pieces of one block
@@ -147,7 +148,7 @@ int64_t stream_ring_entries(int64_t capacity, int max_depth, int64_t max_spp, in
 int wave_iterations(int max_depth);
 // persistent grid sizes from the SM count and occupancy (queries only, no allocation)
 LaunchShape launch_shape();
-LaunchShape launch_shape_variant(bool stack32, bool regcap);
+LaunchShape launch_shape_variant(bool stack32, bool regcap, bool fast_only = false);
 // starts a render: zeroes the counters and sets the admission limit (`limit`; with `waves`
 // nothing is admitted until the first wave's k_wave_next) -- one kernel, so it may run
 // inside a stream capture; the per-pixel counts of the ring must be zero
