@@ -30,20 +30,25 @@ struct NeeRay
 };
 
 // emission picked up when the extension ray misses or hits an emitter
+// LIGHTS: the light kinds a build handles (1 environment, 2 area lights, 3 both); the
+// shading kernel is built per combination, so a render without one kind does not carry
+// its code (the shading kernel misses in the instruction cache) or its registers
+template <int LIGHTS = 3>
 __device__ __forceinline__ float3 miss_emission(const SceneView& S, float3 d, float3 T, bool no_direct)
 {
-    if (no_direct && S.env_w > 0) return T * env_radiance(S, d);
+    if ((LIGHTS & 1) && no_direct && S.env_w > 0) return T * env_radiance(S, d);
     return mk(0.f, 0.f, 0.f);
 }
 
 // next-event rays of one scattering vertex (at most 2 any-hit + 2 closest-hit rays);
 // u: the vertex's NUM_DIMS uniforms.  Returns the number written to out.
+template <int LIGHTS = 3>
 __device__ __forceinline__ int make_nee(const SceneView& S, const Mat& m, float3 wi, float3 ns, float3 phit, float3 T,
                                         const float* u, NeeRay* out)
 {
     int k = 0;
     const float inf = __int_as_float(0x7f800000);
-    if (S.env_w > 0)
+    if ((LIGHTS & 1) && S.env_w > 0)
     {
         // sampleEnvmapUsingLightPDF (demo_pt.cpp:430-465)
         float3 ldir, lrad;
@@ -87,7 +92,7 @@ __device__ __forceinline__ int make_nee(const SceneView& S, const Mat& m, float3
             }
         }
     }
-    if (S.light_area > 0.f)
+    if ((LIGHTS & 2) && S.light_area > 0.f)
     {
         // BSDF sample, MIS against the area lights (demo_pt.cpp:593-614)
         BsdfSample bs = bsdf_sample(m, wi, ns, u[D_AREA_BSDF_0], u[D_AREA_BSDF_1]);

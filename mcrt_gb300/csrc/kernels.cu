@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
 // 32.4 ms, 8 blocks 26.5, 9 blocks 25.0, 10 blocks 26.3.  One build only: builds under
 // different register budgets contract multiply-adds differently, and every
 // configuration must render the same image.
-template <bool ADJ>
+template <bool ADJ, int LIGHTS = 3>
 __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];
@@ -539,7 +539,7 @@ __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
             }
             if (prim < 0)
             {
-                Ladd = miss_emission(S, d, T, no_direct);
+                Ladd = miss_emission<LIGHTS>(S, d, T, no_direct);
             }
             else
             {
@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
                     rstate = rng.state;
                     float3 wi = -d;
                     bool   nee_here = does_nee(m.type);
-                    if (nee_here) n_nee = make_nee(S, m, wi, ns, phit, T, u, nee);
+                    if (nee_here) n_nee = make_nee<LIGHTS>(S, m, wi, ns, phit, T, u, nee);
                     cont = continue_path(m, wi, ns, T, u, depth, J.max_depth, J.rr_depth, T2, cdir);
                     flags2 = (nee_here ? 1 : 0) | ((depth + 1) << 8) | (nlog << 20);
                 }
@@ -1159,7 +1159,14 @@ void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t 
     k_extend<STACK, COUNT, MINB, REFM><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, p);
     end();
     beg(2);
-    k_shade<ADJ><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+    if constexpr (ADJ)
+        k_shade<true><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+    else if (ls.lights == 1)
+        k_shade<false, 1><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+    else if (ls.lights == 2)
+        k_shade<false, 2><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+    else
+        k_shade<false, 3><<<ls.grid_shade, 128, dyn, st>>>(a, p);
     end();
     beg(3);
     k_connect<STACK, COUNT, MINB, ADJ, 0, REFM><<<ls.grid_any, kTraceBlock, dyn, st>>>(a, p);
@@ -1627,8 +1634,14 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     const bool  stack32 = (vb & MCRT_VARIANT_STACK32) && bvh_depth + 2 < 32;
     const bool  regcap = (vb & MCRT_VARIANT_REGCAP) != 0;
     bool        fast_only = true;
-    for (const JobGPU& J : jobs) fast_only = fast_only && J.traverse != MCRT_TRAVERSE_REF;
+    int         lights = 0;
+    for (const JobGPU& J : jobs)
+    {
+        fast_only = fast_only && J.traverse != MCRT_TRAVERSE_REF;
+        lights |= (J.scene.env_w > 0 ? 1 : 0) | (J.scene.light_area > 0.f ? 2 : 0);
+    }
     LaunchShape lsv = launch_shape_variant(stack32, regcap, fast_only);
+    lsv.lights = lights == 0 ? 3 : lights;
     Workspace&  w = owner->ws;
     w.args.batch_fetch = (vb & MCRT_VARIANT_GRIDSTRIDE) ? 0 : 1;
     StageTimer  timer;

@@ -165,6 +165,9 @@ extern "C" int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera,
         k_noalloc_setup<<<static_cast<int>((waves + 256) / 256), 256, 0, st>>>(J, L.job, L.chunks, total, per_wave,
                                                                              waves);
         LaunchShape ls = launch_shape();
+        // the shading build of mcrt_render for this scene, so both render the same image
+        ls.lights = (J.scene.env_w > 0 ? 1 : 0) | (J.scene.light_area > 0.f ? 2 : 0);
+        if (ls.lights == 0) ls.lights = 3;
         enqueue_render_begin(a, true, 0, st);
         for (int64_t k = 0; k < waves; ++k) enqueue_wave_plain(a, params->max_depth, ls, st);
         e = cudaGetLastError();
