@@ -314,9 +314,7 @@ __device__ __forceinline__ bool fast_step(FastTrav& r, const FastNode* nodes, co
             if (watertight(r.wr, xyz(a), xyz(b), xyz(c), r.tmin, r.best, t, u, v))
             {
                 r.best = t;
-                r.hit.t = t;
-                r.hit.u = u;
-                r.hit.v = v;
+                r.hit.t = t;  // u, v: recomputed for the final hit only (refine_hit)
                 r.hit.prim = __float_as_int(a.w);
                 if (any) return true;
             }
@@ -491,10 +489,21 @@ __device__ __forceinline__ bool trace_ref(const SceneView& s, float3 o, float3 d
 __device__ __forceinline__ void refine_hit(const SceneView& s, float3 o, float3 d, float tmin, Hit& hit)
 {
     const float4* pv = s.prim_verts + 3 * hit.prim;
+    const float3  va = xyz(__ldg(pv)), vb = xyz(__ldg(pv + 1)), vc = xyz(__ldg(pv + 2));
     float         t, u, v;
-    if (ref_mt(o, d, xyz(__ldg(pv)), xyz(__ldg(pv + 1)), xyz(__ldg(pv + 2)), t, u, v) && t > tmin)
+    if (ref_mt(o, d, va, vb, vc, t, u, v) && t > tmin)
     {
         hit.t = t;
+        hit.u = u;
+        hit.v = v;
+        return;
+    }
+    // the watertight test's own barycentrics: the traversal keeps only t and the primitive
+    // (two registers fewer in its loop); the same inputs give the same result again
+    hit.u = 0.f;
+    hit.v = 0.f;
+    if (watertight(make_wray(o, d), va, vb, vc, tmin, __int_as_float(0x7f800000), t, u, v))
+    {
         hit.u = u;
         hit.v = v;
     }
