@@ -109,7 +109,7 @@ class ClockSampler:
 # DRAM bytes per average launch of the traversal kernels on the default cfg1 frame
 # (ncu dram__bytes_read.sum + dram__bytes_write.sum over every launch of three frames,
 # warm caches; profiles/cfg1_dram_traffic.md).  Valid only for that exact configuration.
-CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 594.9e6, "k_extend": 473.1e6}
+CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 581.1e6, "k_extend": 459.0e6}
 
 
 def measured_peak_hbm():
@@ -440,8 +440,9 @@ def main():
     ob, oms = kernels[other][0], kernels[other][1]
     other_achieved = (ob / launches_per_render) / (oms / max(extend_launches, 1) / 1e3) / 1e9 if oms > 0 else 0.0
 
-    # e2e: the C-ABI call with host buffers (image copied back inside the call)
-    host_img = np.zeros((cam.height, cam.width, 3), np.float32)
+    # e2e: the C-ABI call with host buffers (image copied back inside the call, into pinned
+    # host memory)
+    host_img = torch.zeros((cam.height, cam.width, 3), dtype=torch.float32, pin_memory=True).numpy()
     e2e_ms, e2e_rays, h2d, d2h = [], 0, 0, 0
     for k in range(max(1, args.steps)):
         flush.zero_()
