@@ -472,8 +472,8 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
         float4        o = a.qo[p][i], d = a.qd[p][i];
         const JobGPU& J = a.jobs[__float_as_int(o.w)];
         Hit           h;
-        bool hit = trace_ray<false, STACK, COUNT, REFM>(J.scene, J.traverse, xyz(o), xyz(d), kEpsRay, inf, st, kTraceBlock, h,
-                                                  a.err, &cnt);
+        bool hit = trace_ray<false, STACK, COUNT, REFM>(J.scene, J.traverse, xyz(o), xyz(d), kEpsRay, inf, st,
+                                                        kTraceBlock, h, a.err, &cnt);
         a.hits[i] = hit_record(hit, h);
     }
     if (COUNT) flush_count(a.stats, 2, cnt);
@@ -723,8 +723,8 @@ __global__ void __launch_bounds__(kTraceBlock, (Q == 0 && MINB > 1) ? kAnyHitMin
         float4        o = a.so[Q][k], d = a.sd[Q][k];
         const JobGPU& J = a.jobs[a.sm[Q][k].w];
         Hit           h;
-        bool hit = trace_ray<Q == 0, STACK, COUNT, REFM>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st, kTraceBlock, h,
-                                                   a.err, &cnt);
+        bool hit = trace_ray<Q == 0, STACK, COUNT, REFM>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st,
+                                                         kTraceBlock, h, a.err, &cnt);
         connect_result<ADJ>(a, G, p, Q, k, hit, h);
     }
     if (COUNT) flush_count(a.stats, 4, cnt);
@@ -1159,14 +1159,12 @@ void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t 
     k_extend<STACK, COUNT, MINB, REFM><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, p);
     end();
     beg(2);
-    if constexpr (ADJ)
-        k_shade<true><<<ls.grid_shade, 128, dyn, st>>>(a, p);
-    else if (ls.lights == 1)
-        k_shade<false, 1><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+    if (ls.lights == 1)
+        k_shade<ADJ, 1><<<ls.grid_shade, 128, dyn, st>>>(a, p);
     else if (ls.lights == 2)
-        k_shade<false, 2><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+        k_shade<ADJ, 2><<<ls.grid_shade, 128, dyn, st>>>(a, p);
     else
-        k_shade<false, 3><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+        k_shade<ADJ, 3><<<ls.grid_shade, 128, dyn, st>>>(a, p);
     end();
     beg(3);
     k_connect<STACK, COUNT, MINB, ADJ, 0, REFM><<<ls.grid_any, kTraceBlock, dyn, st>>>(a, p);
@@ -1482,28 +1480,31 @@ int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<
 // Path-replay adjoint on the streaming wavefront: the forward's stages with ADJ set (see
 // k_shade, k_connect, finish_paths).  Needs max_depth < kAdjLog and material ids that fit
 // the 16-bit log.
-template <int STACK>
+// REFM = false when every job traverses in FAST mode; the shading build follows ls.lights
+// (the forward's specialisations)
+template <int STACK, bool REFM>
 void enqueue_adjoint_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, size_t dyn)
 {
-    enqueue_iter<STACK, false, kTraceMinBlocks, true>(a, p, ls, st, nullptr, dyn);
+    enqueue_iter<STACK, false, kTraceMinBlocks, true, REFM>(a, p, ls, st, nullptr, dyn);
 }
 
-template <int STACK>
+template <int STACK, bool REFM>
 int adjoint_launch_shape(size_t dyn, LaunchShape& ls)
 {
-    CK(cudaFuncSetAttribute(k_regen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
-    CK(cudaFuncSetAttribute(k_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));
+    const int d = static_cast<int>(dyn);
+    CK(cudaFuncSetAttribute(k_regen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
+    CK(cudaFuncSetAttribute(k_shade<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
+    CK(cudaFuncSetAttribute(k_shade<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
+    CK(cudaFuncSetAttribute(k_shade<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
     constexpr int B = kTraceMinBlocks;
-    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            static_cast<int>(dyn)));
-    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            static_cast<int>(dyn)));
+    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 0, REFM>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
+    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 1, REFM>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
     const int sms = num_sms();
     int       occ_e = 0, occ_s = 0, occ_a = 0, occ_c = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_extend<STACK, false, B>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<true>, 128, dyn);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_connect<STACK, false, B, true, 0>, kTraceBlock, dyn);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_connect<STACK, false, B, true, 1>, kTraceBlock, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_extend<STACK, false, B, REFM>, kTraceBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<true, 3>, 128, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_connect<STACK, false, B, true, 0, REFM>, kTraceBlock, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_connect<STACK, false, B, true, 1, REFM>, kTraceBlock, dyn);
     ls.grid_trace = sms * std::max(occ_e, 1);
     ls.grid_any = sms * std::max(occ_a, 1);
     ls.grid_connect = sms * std::max(occ_c, 1);
@@ -1544,14 +1545,27 @@ int adjoint_stream(Workspace& w, const std::vector<JobGPU>& jobs, int64_t total,
     a.grad_shared = gbytes <= 64 * 1024 ? 1 : 0;
     const size_t dyn = a.grad_shared ? gbytes : 0;
     const bool   stack32 = bvh_depth + 2 < 32;
-    LaunchShape  ls;
-    rc = stack32 ? adjoint_launch_shape<32>(dyn, ls) : adjoint_launch_shape<kStack>(dyn, ls);
+    bool         fast_only = true;
+    int          lights = 0;
+    for (const JobGPU& J : jobs)
+    {
+        fast_only = fast_only && J.traverse != MCRT_TRAVERSE_REF;
+        lights |= (J.scene.env_w > 0 ? 1 : 0) | (J.scene.light_area > 0.f ? 2 : 0);
+    }
+    LaunchShape ls;
+    rc = stack32 ? (fast_only ? adjoint_launch_shape<32, false>(dyn, ls) : adjoint_launch_shape<32, true>(dyn, ls))
+                 : (fast_only ? adjoint_launch_shape<kStack, false>(dyn, ls)
+                              : adjoint_launch_shape<kStack, true>(dyn, ls));
     if (rc) return rc;
+    ls.fast_only = fast_only;
+    ls.lights = lights == 0 ? 3 : lights;
     auto iter = [&](cudaStream_t s2, int p, StageTimer*) {
         if (stack32)
-            enqueue_adjoint_iter<32>(a, p, ls, s2, dyn);
+            fast_only ? enqueue_adjoint_iter<32, false>(a, p, ls, s2, dyn)
+                      : enqueue_adjoint_iter<32, true>(a, p, ls, s2, dyn);
         else
-            enqueue_adjoint_iter<kStack>(a, p, ls, s2, dyn);
+            fast_only ? enqueue_adjoint_iter<kStack, false>(a, p, ls, s2, dyn)
+                      : enqueue_adjoint_iter<kStack, true>(a, p, ls, s2, dyn);
     };
     StageTimer timer;
     return stream_loop(w, a, total, max_depth, false, true, st, timer, run, iter);
