@@ -213,3 +213,25 @@ def test_consistent_normals_match_oracle(cuda_device):
     desc2 = scenes.cfg0_scene(sphere_level=1)
     desc2.materials[-1].type = SPEC | CONSISTENT
     np.testing.assert_array_equal(GpuScene(desc2).render(cam, **kw)[0], gpu)
+
+
+def test_area_and_environment_lights_in_one_scene(cuda_device):
+    """Both light kinds in one render (the shading build for both): the Cornell box, open
+    towards the camera, under a sky with a sun, against the float oracle with the same
+    random numbers; then batched with an area-light-only job (both jobs run the build for
+    both kinds), each image as that job renders alone."""
+    from mcrt_gb300 import GpuScene, render_batch, scenes
+    from oracle.oracle import OracleScene
+    desc, cam = _cfg0(32)
+    desc.envmap = scenes.sky_envmap(64, 32, sun_radiance=50.0, sun_diameter_deg=8.0)
+    kw = dict(spp=16, max_depth=6, rr_depth=3, seed=9)
+    both = GpuScene(desc)
+    gpu, _ = both.render(cam, **kw)
+    ref = OracleScene(desc, 32).render(cam.as_array(), 32, 32, 16, 6, 3, seed=9)
+    _crn_compare(gpu, ref["mean"].astype(np.float32), "area+env")
+    area_desc, area_cam = _cfg0(16)
+    area = GpuScene(area_desc)
+    outs, _ = render_batch([area, both], [area_cam, cam], [kw, kw])
+    for o, alone in zip(outs, [area.render(area_cam, **kw)[0], gpu]):
+        close = np.mean(np.abs(o - alone) / (np.abs(alone) + 1e-3) < 1e-3)
+        assert close > 0.98, close
