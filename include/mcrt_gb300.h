@@ -6,7 +6,10 @@
  * the boundary; mcrt_last_error() returns the message of the calling thread's last
  * failure.  Device memory for a scene is owned by the library; the caller owns all
  * buffers it passes in.  A scene handle may be used from several host threads as
- * long as each thread uses its own CUDA stream.
+ * long as each thread uses its own CUDA stream.  Renders on one device share one
+ * working-memory block (the ray queues, up to about 50 GB at the default 64 M-ray queue;
+ * it grows to the largest render and is kept until the process exits), so they run one
+ * after another.  Where that block cannot be allocated, the default queue halves itself.
  *
  * Reference interfaces replaced (paths are relative to the MCRT source tree):
  *   SceneBVH::SceneBVH            src/core/scenebvh.h:14, scenebvh.cpp:404-444 -> mcrt_scene_create

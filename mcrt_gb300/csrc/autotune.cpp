@@ -4,7 +4,7 @@
 // The search is two-stage, so it costs about eight probe renders (each best of two):
 //   1. traversal kernel variants at the default queue capacity: 32-entry or 64-entry
 //      shared-memory stacks, 56-register cap or none, warp batch fetch or grid stride;
-//   2. queue capacities (2^21 .. 2^24 rays) with the best variant.
+//   2. queue capacities (2^21 .. 2^26 rays) with the best variant.
 // Every configuration renders the same image (the schedule never changes a path's
 // arithmetic), so only the time is compared.
 #include <cuda_runtime.h>
@@ -42,13 +42,13 @@ extern "C" int mcrt_autotune(int32_t num_jobs, mcrt_scene* const* scenes, const 
             int rc = validate_job(scenes[j], &cameras[j], &params[j]);
             if (rc) return rc;
         }
-        // probe: the same jobs with spp scaled so that the probe holds about four of the
+        // probe: the same jobs with spp scaled so that the probe holds about two of the
         // largest candidate queues of paths (or the whole render if it is smaller)
-        constexpr int64_t kMaxCapacity = int64_t(1) << 24;
+        constexpr int64_t kMaxCapacity = int64_t(1) << 26;
         int64_t           total = 0;
         for (int j = 0; j < num_jobs; ++j)
             total += static_cast<int64_t>(cameras[j].width) * cameras[j].height * params[j].spp;
-        const double                    scale = std::min(1.0, 4.0 * kMaxCapacity / static_cast<double>(total));
+        const double                    scale = std::min(1.0, 2.0 * kMaxCapacity / static_cast<double>(total));
         std::vector<mcrt_render_params> probe(params, params + num_jobs);
         int64_t                         probe_paths = 0;
         for (int j = 0; j < num_jobs; ++j)

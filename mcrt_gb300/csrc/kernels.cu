@@ -953,20 +953,25 @@ struct Workspace
     unsigned long long* h_poll = nullptr;  // pinned: completion polls of the streaming schedule
     int64_t             adj_capacity = 0;    // rays per queue of `adj_block`
     void*               adj_block = nullptr; // adjoint vertex logs
-    void release()
-    {
-        cudaFree(adj_block);
-        cudaFree(block);
-        cudaFree(ring_block);
-        cudaFree(jobs);
-        cudaFree(chunk_table);
-        cudaFree(ctrl);
-        cudaFree(stats);
-        cudaFree(err);
-        cudaFreeHost(h_poll);
-        *this = Workspace{};
-    }
 };
+
+// One workspace per device, shared by every scene on it.  A render's queues and ring are
+// its largest allocation (about 50 GB at the default 64 M-ray queue); kept per scene, they
+// multiplied by the number of scenes a process holds (the 64-scene mix rendered scene by
+// scene would have kept 412 GB).  A render takes its device's mutex (renders on one device
+// share it anyway); the workspace grows to the largest render and lives until the process
+// exits.
+constexpr int kMaxDevices = 64;
+struct DeviceWorkspace
+{
+    std::mutex mu;
+    Workspace  ws;
+};
+DeviceWorkspace& device_workspace(int device)
+{
+    static DeviceWorkspace pool[kMaxDevices];
+    return pool[device];
+}
 
 }  // namespace
 
@@ -982,7 +987,6 @@ struct mcrt_scene
     std::vector<int64_t> array_bytes;  // bytes of each uploaded array, in upload order
     uint64_t             desc_hash = 0;  // of the description the scene was built from
     int*               d_err = nullptr;
-    Workspace          ws;
     std::mutex         mu;
 };
 
@@ -1467,9 +1471,21 @@ int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<
     capacity = std::max<int64_t>(capacity, 64);
     int64_t max_spp = 1;
     for (int64_t v : pix_spp) max_spp = std::max(max_spp, v);
-    const int64_t ring = stream_ring_entries(capacity, max_depth, max_spp, total);
-    WaveArgs      a;
-    int           rc = begin_run(w, jobs, capacity, ring, 0, st, run, a);
+    WaveArgs a;
+    int      rc;
+    for (;;)
+    {
+        const int64_t ring = stream_ring_entries(capacity, max_depth, max_spp, total);
+        rc = begin_run(w, jobs, capacity, ring, 0, st, run, a);
+        // the default capacity halves itself when the device has not the memory for it
+        if (rc == MCRT_ERR_OUT_OF_MEMORY && path_chunk <= 0 && capacity > kMinDefaultQueue)
+        {
+            cudaGetLastError();
+            capacity /= 2;
+            continue;
+        }
+        break;
+    }
     if (rc) return rc;
     auto iter = [&](cudaStream_t s2, int p, StageTimer* tm) {
         with_variant(stack32, regcap, count, IterEnqueue{&a, p, &lsv, s2, tm});
@@ -1521,16 +1537,38 @@ int adjoint_stream(Workspace& w, const std::vector<JobGPU>& jobs, int64_t total,
     capacity = std::min(capacity, (total + 31) / 32 * 32);
     capacity = std::max<int64_t>(capacity, 64);
     WaveArgs a;
-    int      rc = begin_run(w, jobs, capacity, 0, 0, st, run, a);
-    if (rc) return rc;
-    if (w.adj_capacity < capacity)
+    int      rc;
+    for (;;)
     {
-        cudaFree(w.adj_block);
-        w.adj_block = nullptr;
-        w.adj_capacity = 0;
-        CK(cudaMalloc(&w.adj_block, 4 * (32 * static_cast<size_t>(capacity) + 256)));
-        w.adj_capacity = capacity;
+        rc = begin_run(w, jobs, capacity, 0, 0, st, run, a);
+        if (rc == MCRT_OK && w.adj_capacity < capacity)
+        {
+            cudaFree(w.adj_block);
+            w.adj_block = nullptr;
+            w.adj_capacity = 0;
+            if (cudaMalloc(&w.adj_block, 4 * (32 * static_cast<size_t>(capacity) + 256)) == cudaSuccess)
+            {
+                w.adj_capacity = capacity;
+            }
+            else
+            {
+                w.adj_block = nullptr;
+                cudaEventDestroy(run.e0);
+                cudaEventDestroy(run.e1);
+                run.e0 = run.e1 = nullptr;
+                rc = fail(MCRT_ERR_OUT_OF_MEMORY, "adjoint vertex log allocation failed");
+            }
+        }
+        // the default capacity halves itself when the device has not the memory for it
+        if (rc == MCRT_ERR_OUT_OF_MEMORY && path_chunk <= 0 && capacity > kMinDefaultQueue)
+        {
+            cudaGetLastError();
+            capacity /= 2;
+            continue;
+        }
+        break;
     }
+    if (rc) return rc;
     Carver c{static_cast<char*>(w.adj_block)};
     for (int k = 0; k < 2; ++k)
     {
@@ -1581,7 +1619,10 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
         if (!outs[j]) return fail(MCRT_ERR_INVALID_ARGUMENT, "null image buffer");
     }
     mcrt_scene* owner = scenes[0];
+    if (owner->device < 0 || owner->device >= kMaxDevices) return fail(MCRT_ERR_INVALID_ARGUMENT, "device index");
     std::lock_guard<std::mutex> lock(owner->mu);
+    DeviceWorkspace&            dw = device_workspace(owner->device);
+    std::lock_guard<std::mutex> wlock(dw.mu);
     CK(cudaSetDevice(owner->device));
     const mcrt_render_params& p0 = params[0];
     int                       ptr_mode = p0.ptr_mode;
@@ -1656,7 +1697,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     }
     LaunchShape lsv = launch_shape_variant(stack32, regcap, fast_only);
     lsv.lights = lights == 0 ? 3 : lights;
-    Workspace&  w = owner->ws;
+    Workspace&  w = dw.ws;
     w.args.batch_fetch = (vb & MCRT_VARIANT_GRIDSTRIDE) ? 0 : 1;
     StageTimer  timer;
     RunResult   run;
@@ -1969,7 +2010,6 @@ int mcrt_scene_destroy(mcrt_scene* s)
     if (!s) return MCRT_OK;
     cudaSetDevice(s->device);
     for (void* p : s->allocs) cudaFree(p);
-    s->ws.release();
     delete s;
     return MCRT_OK;
 }
@@ -2163,8 +2203,11 @@ static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_came
     }
     if ((n_albedo > 0 && !d_albedo) || (n_emis > 0 && !d_emis) || n_albedo < 0 || n_emis < 0)
         return fail(MCRT_ERR_INVALID_ARGUMENT, "null gradient buffer");
-    mcrt_scene*                 owner = scenes[0];
+    mcrt_scene* owner = scenes[0];
+    if (owner->device < 0 || owner->device >= kMaxDevices) return fail(MCRT_ERR_INVALID_ARGUMENT, "device index");
     std::lock_guard<std::mutex> lock(owner->mu);
+    DeviceWorkspace&            dw = device_workspace(owner->device);
+    std::lock_guard<std::mutex> wlock(dw.mu);
     CK(cudaSetDevice(owner->device));
     std::vector<void*> temp;
     auto               cleanup = [&]() {
@@ -2230,7 +2273,7 @@ static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_came
         dga = static_cast<float*>(a2);
         dge = static_cast<float*>(a3);
     }
-    Workspace& w = owner->ws;
+    Workspace& w = dw.ws;
     // the wavefront replay (default) needs the vertex log to hold every vertex and 16-bit
     // material ids; otherwise, or with MCRT_SCHEDULE_WAVES, one thread replays each path
     int  max_depth = 0, bvh_depth = 0;

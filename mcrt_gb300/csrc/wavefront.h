@@ -41,7 +41,12 @@ constexpr int kTraceMinBlocks = 9;
 constexpr int kAnyHitMinBlocks = 10;
 constexpr int kMaxDepth = 62;
 constexpr int64_t kMaxQueue = int64_t(1) << 27;     // rays per queue (result indices stay in int)
-constexpr int64_t kDefaultQueue = int64_t(1) << 24;  // streaming schedule default (12 GB of queues)
+// Streaming schedule default: 64 M rays (49 GB of queues).  Per cfg1 frame (67 M paths):
+// 1 / 2 / 4 / 8 / 16 / 32 / 64 M rays 184.6 / 146.9 / 128.1 / 118.3 / 113.4 / 111.4 /
+// 109.5 ms -- fewer, longer launches amortise each launch's ramp and tail.  If its
+// allocation fails the default halves itself, down to kMinDefaultQueue.
+constexpr int64_t kDefaultQueue = int64_t(1) << 26;
+constexpr int64_t kMinDefaultQueue = int64_t(1) << 20;
 
 // counters of one render
 struct Ctrl
