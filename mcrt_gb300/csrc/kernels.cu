@@ -1257,9 +1257,11 @@ void with_variant(bool stack32, bool regcap, bool count, const F& f)
     else if (stack32)
     {
         if (regcap)
-            count ? f.template run<32, true, B, false>() : f.template run<32, false, B, false>();
+            count ? f.template run<kSmallStack, true, B, false>()
+                  : f.template run<kSmallStack, false, B, false>();
         else
-            count ? f.template run<32, true, 1, false>() : f.template run<32, false, 1, false>();
+            count ? f.template run<kSmallStack, true, 1, false>()
+                  : f.template run<kSmallStack, false, 1, false>();
     }
     else
     {
@@ -1582,7 +1584,7 @@ int adjoint_stream(Workspace& w, const std::vector<JobGPU>& jobs, int64_t total,
     const size_t gbytes = sizeof(float) * 3 * static_cast<size_t>(na + ne);
     a.grad_shared = gbytes <= 64 * 1024 ? 1 : 0;
     const size_t dyn = a.grad_shared ? gbytes : 0;
-    const bool   stack32 = bvh_depth + 2 < 32;
+    const bool   stack32 = bvh_depth + 2 < kSmallStack;
     bool         fast_only = true;
     int          lights = 0;
     for (const JobGPU& J : jobs)
@@ -1591,7 +1593,8 @@ int adjoint_stream(Workspace& w, const std::vector<JobGPU>& jobs, int64_t total,
         lights |= (J.scene.env_w > 0 ? 1 : 0) | (J.scene.light_area > 0.f ? 2 : 0);
     }
     LaunchShape ls;
-    rc = stack32 ? (fast_only ? adjoint_launch_shape<32, false>(dyn, ls) : adjoint_launch_shape<32, true>(dyn, ls))
+    rc = stack32 ? (fast_only ? adjoint_launch_shape<kSmallStack, false>(dyn, ls)
+                              : adjoint_launch_shape<kSmallStack, true>(dyn, ls))
                  : (fast_only ? adjoint_launch_shape<kStack, false>(dyn, ls)
                               : adjoint_launch_shape<kStack, true>(dyn, ls));
     if (rc) return rc;
@@ -1599,8 +1602,8 @@ int adjoint_stream(Workspace& w, const std::vector<JobGPU>& jobs, int64_t total,
     ls.lights = lights == 0 ? 3 : lights;
     auto iter = [&](cudaStream_t s2, int p, StageTimer*) {
         if (stack32)
-            fast_only ? enqueue_adjoint_iter<32, false>(a, p, ls, s2, dyn)
-                      : enqueue_adjoint_iter<32, true>(a, p, ls, s2, dyn);
+            fast_only ? enqueue_adjoint_iter<kSmallStack, false>(a, p, ls, s2, dyn)
+                      : enqueue_adjoint_iter<kSmallStack, true>(a, p, ls, s2, dyn);
         else
             fast_only ? enqueue_adjoint_iter<kStack, false>(a, p, ls, s2, dyn)
                       : enqueue_adjoint_iter<kStack, true>(a, p, ls, s2, dyn);
@@ -1686,7 +1689,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     // traversal registers capped for kTraceMinBlocks blocks per SM);
     // MCRT_VARIANT_EXPLICIT: the given bits
     const int   vb = (p0.variant & MCRT_VARIANT_EXPLICIT) ? p0.variant : (MCRT_VARIANT_STACK32 | MCRT_VARIANT_REGCAP);
-    const bool  stack32 = (vb & MCRT_VARIANT_STACK32) && bvh_depth + 2 < 32;
+    const bool  stack32 = (vb & MCRT_VARIANT_STACK32) && bvh_depth + 2 < kSmallStack;
     const bool  regcap = (vb & MCRT_VARIANT_REGCAP) != 0;
     bool        fast_only = true;
     int         lights = 0;
@@ -1833,9 +1836,11 @@ LaunchShape launch_shape_variant(bool stack32, bool regcap, bool fast_only)
     else if (stack32)
     {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ_t, regcap ? k_extend<32, false, B, false> : k_extend<32, false, 1, false>, kTraceBlock, 0);
+            &occ_t, regcap ? k_extend<kSmallStack, false, B, false> : k_extend<kSmallStack, false, 1, false>,
+            kTraceBlock, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &occ_a, regcap ? k_connect<32, false, B, false, 0, false> : k_connect<32, false, 1, false, 0, false>,
+            &occ_a,
+            regcap ? k_connect<kSmallStack, false, B, false, 0, false> : k_connect<kSmallStack, false, 1, false, 0, false>,
             kTraceBlock, 0);
     }
     else

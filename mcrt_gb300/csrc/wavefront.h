@@ -30,6 +30,8 @@ namespace mcrt {
 
 constexpr int kTraceBlock = 128;
 constexpr int kStack = 64;
+// the smaller traversal stack, used when the tree is shallow enough (MCRT_VARIANT_STACK32)
+constexpr int kSmallStack = 32;
 // Traversal kernels under MCRT_VARIANT_REGCAP: __launch_bounds__(kTraceBlock, kTraceMinBlocks)
 // caps them at 56 registers, so 9 blocks (36 warps) fit an SM.  Measured on the cfg1 frame:
 // 8 blocks (64 registers) 52.6 / 59.9 ms extend / connect, 9 blocks 52.2 / 56.7, 10 blocks
