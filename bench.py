@@ -112,6 +112,10 @@ class ClockSampler:
 CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 718.3e6, "k_extend": 568.8e6}
 
 
+# rows of the cfg0 / cfg1 frames the CPU port renders for cpu_baseline and --impl reference
+CPU_BASELINE_ROWS = {"cfg0": (64, 192), "cfg1": (384, 640)}
+
+
 def measured_peak_hbm():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -158,20 +162,19 @@ def run_reference(args):
     from oracle.oracle import OracleScene
     desc, cam, p, text = workload(args.workload)
     cores = os.cpu_count() or 1
-    # bands of rows per step, a few seconds of CPU work each; at least one row per core
-    rows_per_step = max(cores, {"cfg0": 64, "cfg1": 96}.get(args.workload, 96))
+    # every step renders the same band of rows as the bench's cpu_baseline (a few seconds of
+    # CPU work), with its own seed: the rate does not depend on how many steps run
+    r0, r1 = CPU_BASELINE_ROWS.get(args.workload, CPU_BASELINE_ROWS["cfg1"])
     osc = OracleScene(desc, 32)  # scene and BVH built once, outside the timed steps
     kind = "port"
     times, rays_total = [], 0
     for step in range(args.warmup + args.steps):
-        r0 = (step * rows_per_step) % cam.height
-        rays, paths, dt, _ = cpu_port_sample(desc, cam, p, (r0, min(cam.height, r0 + rows_per_step)), seed=step,
-                                             osc=osc)
+        rays, paths, dt, _ = cpu_port_sample(desc, cam, p, (r0, r1), seed=step, osc=osc)
         if step >= args.warmup:
             times.append(dt)
             rays_total += rays
     value = rays_total / sum(times) / 1e6
-    sample = (f"{args.workload} bands of {rows_per_step} rows x {cam.width} px x {p['spp']} spp per step "
+    sample = (f"{args.workload} rows {r0}-{r1} x {cam.width} px x {p['spp']} spp per step "
               f"(float port of the estimator, {cores} threads)")
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(times) / len(times), 3),
@@ -459,7 +462,7 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rows = {"cfg0": (64, 192), "cfg1": (384, 640)}[args.workload]
+        rows = CPU_BASELINE_ROWS[args.workload]
         c_rays, c_paths, c_dt, c_build = cpu_port_sample(desc, cam, p, rows)
         cpu = {"value": round(c_rays / c_dt / 1e6, 3), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                "sample": f"{args.workload} rows {rows[0]}-{rows[1]} x {cam.width} px x {p['spp']} spp "
