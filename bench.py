@@ -475,11 +475,10 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (procedural scene, seeded)",
             "config": {"workload": text, "traversal": args.traverse, "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"replicas x{world}", "schedule": args.schedule,
-                       "path_slots": args.path_chunk or "default", "variant": args.variant,
-                       "leaf_size": args.leaf_size or 2,
-                       "autotuned": tune is not None,
-                       "waves_or_iterations_per_step": st_last["waves"],
-                       "scene_setup_s": round(setup_s, 2), "scene_device_bytes": sc.info()["device_bytes"], "fast_nodes": sc.info()["fast_nodes"]},
+                       "path_slots": args.path_chunk or "default (67108864, clamped to the paths)",
+                       "variant": args.variant, "leaf_size": args.leaf_size or 2, "autotuned": tune is not None,
+                       "waves_or_iterations_per_step": st_last["waves"], "scene_setup_s": round(setup_s, 2),
+                       "scene_device_bytes": sc.info()["device_bytes"], "fast_nodes": sc.info()["fast_nodes"]},
             "msamples_per_s": round(msamples, 3),
             "rays_per_path": round(rays / max(paths, 1), 3),
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
