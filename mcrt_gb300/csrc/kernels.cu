@@ -1172,7 +1172,8 @@ void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t 
     end();
     beg(3);
     k_connect<STACK, COUNT, MINB, ADJ, 0, REFM><<<ls.grid_any, kTraceBlock, dyn, st>>>(a, p);
-    k_connect<STACK, COUNT, MINB, ADJ, 1, REFM><<<ls.grid_connect, kTraceBlock, dyn, st>>>(a, p);
+    // closest-hit next-event rays exist only where a job has area lights
+    if (ls.lights & 2) k_connect<STACK, COUNT, MINB, ADJ, 1, REFM><<<ls.grid_connect, kTraceBlock, dyn, st>>>(a, p);
     end();
 }
 
@@ -1214,6 +1215,7 @@ struct RunResult
     int64_t     launches = 0;
     int64_t     extend_launches = 0;
     int64_t     table_bytes = 0;  // host -> device besides the job table
+    int         iter_launches = 6;  // launches per iteration (5 without area lights)
     int64_t     poll_bytes = 0;   // device -> host completion polls
 };
 
@@ -1341,7 +1343,7 @@ int run_waves(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<i
     run.table_bytes = 8 * static_cast<int64_t>(table.size());
     const int iters = wave_iterations(max_depth);
     run.waves = num_chunks;
-    run.launches = 1 + num_chunks * (1 + 6 * iters);
+    run.launches = 1 + num_chunks * (1 + run.iter_launches * iters);
     run.extend_launches = num_chunks * iters;
     auto enqueue = [&](cudaStream_t s2, StageTimer* tm) {
         with_variant(stack32, regcap, count, WaveEnqueue{&a, max_depth, &lsv, s2, tm});
@@ -1458,7 +1460,7 @@ int stream_loop(Workspace& w, const WaveArgs& a, int64_t total, int max_depth, b
     release_graph();
     if (e != cudaSuccess) return fail(MCRT_ERR_CUDA, std::string("streaming render: ") + cudaGetErrorString(e));
     run.waves = iters;
-    run.launches += iters * 6;
+    run.launches += iters * run.iter_launches;
     run.extend_launches = iters;
     return MCRT_OK;
 }
@@ -1600,6 +1602,7 @@ int adjoint_stream(Workspace& w, const std::vector<JobGPU>& jobs, int64_t total,
     if (rc) return rc;
     ls.fast_only = fast_only;
     ls.lights = lights == 0 ? 3 : lights;
+    run.iter_launches = (ls.lights & 2) ? 6 : 5;
     auto iter = [&](cudaStream_t s2, int p, StageTimer*) {
         if (stack32)
             fast_only ? enqueue_adjoint_iter<kSmallStack, false>(a, p, ls, s2, dyn)
@@ -1704,6 +1707,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     w.args.batch_fetch = (vb & MCRT_VARIANT_GRIDSTRIDE) ? 0 : 1;
     StageTimer  timer;
     RunResult   run;
+    run.iter_launches = (lsv.lights & 2) ? 6 : 5;
     int         rc = p0.schedule == MCRT_SCHEDULE_WAVES
                          ? run_waves(w, jobs, pix_spp, total, max_depth, p0.path_chunk, stack32, regcap, count, stages,
                                      graph, lsv, st, timer, run)

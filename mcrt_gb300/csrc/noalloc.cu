@@ -186,7 +186,7 @@ extern "C" int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera,
             stats->shadow_rays = static_cast<int64_t>(hstats[1]);
             stats->waves = static_cast<int32_t>(waves);
             const int iters = wave_iterations(params->max_depth);
-            stats->kernel_launches = static_cast<int32_t>(2 + waves * (1 + 6 * iters));
+            stats->kernel_launches = static_cast<int32_t>(2 + waves * (1 + ((ls.lights & 2) ? 6 : 5) * iters));
             stats->extend_launches = static_cast<int32_t>(waves * iters);
             stats->d2h_bytes = static_cast<int64_t>(sizeof(hstats) + sizeof(herr));
         }
