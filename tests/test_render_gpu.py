@@ -235,3 +235,18 @@ def test_area_and_environment_lights_in_one_scene(cuda_device):
     for o, alone in zip(outs, [area.render(area_cam, **kw)[0], gpu]):
         close = np.mean(np.abs(o - alone) / (np.abs(alone) + 1e-3) < 1e-3)
         assert close > 0.98, close
+
+
+def test_fast_only_builds_render_the_general_builds_image(cuda_device):
+    """A render whose jobs all traverse in FAST mode runs traversal kernels built without the
+    reference-order traversal; batched with a REF job, the same FAST job runs the general
+    build (64-entry stacks, no register cap).  Its image is the same bit for bit."""
+    from mcrt_gb300 import TRAVERSE_FAST, TRAVERSE_REF, GpuScene, render_batch, scenes
+    desc = scenes.cfg1_scene(level=5, env_size=(256, 128), patch_tris=64)
+    cam = scenes.cfg1_camera(32, 32)
+    fast, ref = GpuScene(desc), GpuScene(desc)  # same light kinds: the same shading build
+    kw = dict(spp=8, max_depth=6, seed=5)
+    alone, _ = fast.render(cam, traverse=TRAVERSE_FAST, **kw)
+    outs, _ = render_batch([fast, ref], [cam, cam],
+                           [dict(kw, traverse=TRAVERSE_FAST), dict(kw, traverse=TRAVERSE_REF)])
+    np.testing.assert_array_equal(outs[0], alone)
