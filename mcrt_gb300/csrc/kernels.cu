@@ -486,18 +486,63 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
 // 32.4 ms, 8 blocks 26.5, 9 blocks 25.0, 10 blocks 26.3.  One build only: builds under
 // different register budgets contract multiply-adds differently, and every
 // configuration must render the same image.
+// Shading class of queue entry i: 0 a miss, 1-6 the hit material (light, Lambert, mirror,
+// dielectric, Phong, GGX).
+__device__ __forceinline__ int shade_class(const WaveArgs& a, int p, int i)
+{
+    const int prim = __float_as_int(a.hits[i].w);
+    if (prim < 0) return 0;
+    const SceneView& S = a.jobs[__float_as_int(a.qo[p][i].w)].scene;
+    const int        t = S.materials[__float_as_int(__ldg(S.prim_shade + 3 * prim).w)].type & 0xff;
+    return t == MAT_GGX ? 6 : min(t, MAT_GLSY) + 1;
+}
+
+// The block's 128 queue entries from `base` on, reordered by shading class (a counting
+// sort in shared memory; entries past n last), so that a warp runs one material's code
+// with all its lanes.  Returns this thread's entry.  The order of the entries changes
+// nothing a path computes: finished samples go to ring slots of their own.
+__device__ __forceinline__ int shade_order(const WaveArgs& a, int p, int base, int n, int* s_base, int* s_perm)
+{
+    const int i0 = base + threadIdx.x;
+    const int key = i0 < n ? shade_class(a, p, i0) : 7;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < 8) s_base[threadIdx.x] = 0;
+    __syncthreads();
+    const unsigned same = __match_any_sync(0xffffffffu, key);
+    const int      lead = __ffs(same) - 1;
+    int            off = 0;
+    if (lane == lead) off = atomicAdd(&s_base[key], __popc(same));
+    off = __shfl_sync(0xffffffffu, off, lead) + __popc(same & lanemask_lt());
+    __syncthreads();
+    if (threadIdx.x < 32)  // exclusive scan of the eight class counts
+    {
+        const int c = lane < 8 ? s_base[lane] : 0;
+        int       incl = c;
+        for (int d = 1; d < 8; d <<= 1)
+        {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        if (lane < 8) s_base[lane] = incl - c;
+    }
+    __syncthreads();
+    s_perm[s_base[key] + off] = i0;
+    __syncthreads();
+    return s_perm[threadIdx.x];
+}
+
 template <bool ADJ, int LIGHTS = 3>
 __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];
+    __shared__ int s_base[8], s_perm[128];
     const Grads G = grads_begin<ADJ>(a, sgrad);
     const int n = min(a.ctrl->qcount[p], static_cast<int>(a.capacity));
     const int lane = threadIdx.x & 31;
-    const int warps_total = (gridDim.x * blockDim.x) >> 5;
     const int pn = p ^ 1;
-    for (int wbase = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < n; wbase += warps_total * 32)
+    for (int bbase = blockIdx.x * 128; bbase < n; bbase += gridDim.x * 128)  // blocks of 128 threads
     {
-        int      i = wbase + lane;
+        int      i = shade_order(a, p, bbase, n, s_base, s_perm);
         bool     valid = i < n;
         bool     cont = false;
         float3   phit = mk(0.f, 0.f, 0.f), cdir = mk(0.f, 0.f, 1.f), T2 = mk(0.f, 0.f, 0.f);
