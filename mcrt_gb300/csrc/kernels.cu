@@ -486,6 +486,9 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
 // 32.4 ms, 8 blocks 26.5, 9 blocks 25.0, 10 blocks 26.3.  One build only: builds under
 // different register budgets contract multiply-adds differently, and every
 // configuration must render the same image.
+// k_shade sorts windows of kShadeWindow queue entries and shades them in rounds of 128.
+constexpr int kShadeRounds = 4, kShadeWindow = 128 * kShadeRounds;
+
 // Shading class of queue entry i: 0 a miss, 1-6 the hit material (light, Lambert, mirror,
 // dielectric, Phong, GGX).
 __device__ __forceinline__ int shade_class(const WaveArgs& a, int p, int i)
@@ -497,22 +500,32 @@ __device__ __forceinline__ int shade_class(const WaveArgs& a, int p, int i)
     return t == MAT_GGX ? 6 : min(t, MAT_GLSY) + 1;
 }
 
-// The block's 128 queue entries from `base` on, reordered by shading class (a counting
-// sort in shared memory; entries past n last), so that a warp runs one material's code
-// with all its lanes.  Returns this thread's entry.  The order of the entries changes
-// nothing a path computes: finished samples go to ring slots of their own.
-__device__ __forceinline__ int shade_order(const WaveArgs& a, int p, int base, int n, int* s_base, int* s_perm)
+// The block's kShadeWindow queue entries from `base` on, reordered by shading class (a
+// counting sort in shared memory; entries past n last), so that a warp runs one
+// material's code with all its lanes.  s_perm receives the entries in sorted order; the
+// block then shades them in rounds of 128.  The order of the entries changes nothing a
+// path computes: finished samples go to ring slots of their own.
+__device__ __forceinline__ void shade_order(const WaveArgs& a, int p, int base, int n, int* s_base, int* s_perm)
 {
-    const int i0 = base + threadIdx.x;
-    const int key = i0 < n ? shade_class(a, p, i0) : 7;
     const int lane = threadIdx.x & 31;
+    int       key[kShadeRounds], off[kShadeRounds];
+#pragma unroll
+    for (int r = 0; r < kShadeRounds; ++r)
+    {
+        const int i0 = base + r * 128 + threadIdx.x;
+        key[r] = i0 < n ? shade_class(a, p, i0) : 7;
+    }
     if (threadIdx.x < 8) s_base[threadIdx.x] = 0;
     __syncthreads();
-    const unsigned same = __match_any_sync(0xffffffffu, key);
-    const int      lead = __ffs(same) - 1;
-    int            off = 0;
-    if (lane == lead) off = atomicAdd(&s_base[key], __popc(same));
-    off = __shfl_sync(0xffffffffu, off, lead) + __popc(same & lanemask_lt());
+#pragma unroll
+    for (int r = 0; r < kShadeRounds; ++r)
+    {
+        const unsigned same = __match_any_sync(0xffffffffu, key[r]);
+        const int      lead = __ffs(same) - 1;
+        int            o = 0;
+        if (lane == lead) o = atomicAdd(&s_base[key[r]], __popc(same));
+        off[r] = __shfl_sync(0xffffffffu, o, lead) + __popc(same & lanemask_lt());
+    }
     __syncthreads();
     if (threadIdx.x < 32)  // exclusive scan of the eight class counts
     {
@@ -526,23 +539,27 @@ __device__ __forceinline__ int shade_order(const WaveArgs& a, int p, int base, i
         if (lane < 8) s_base[lane] = incl - c;
     }
     __syncthreads();
-    s_perm[s_base[key] + off] = i0;
+#pragma unroll
+    for (int r = 0; r < kShadeRounds; ++r) s_perm[s_base[key[r]] + off[r]] = base + r * 128 + threadIdx.x;
     __syncthreads();
-    return s_perm[threadIdx.x];
 }
 
 template <bool ADJ, int LIGHTS = 3>
 __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];
-    __shared__ int s_base[8], s_perm[128];
+    __shared__ int s_base[8], s_perm[kShadeWindow];
     const Grads G = grads_begin<ADJ>(a, sgrad);
     const int n = min(a.ctrl->qcount[p], static_cast<int>(a.capacity));
     const int lane = threadIdx.x & 31;
     const int pn = p ^ 1;
-    for (int bbase = blockIdx.x * 128; bbase < n; bbase += gridDim.x * 128)  // blocks of 128 threads
+    // pos: the first entry of this round; windows start at multiples of kShadeWindow, and a
+    // window's valid entries fill its first rounds (the sort puts entries past n last)
+    for (int pos = blockIdx.x * kShadeWindow; pos < n;)  // blocks of 128 threads
     {
-        int      i = shade_order(a, p, bbase, n, s_base, s_perm);
+        const int round = (pos % kShadeWindow) / 128;
+        if (round == 0) shade_order(a, p, pos, n, s_base, s_perm);
+        int      i = s_perm[round * 128 + threadIdx.x];
         bool     valid = i < n;
         bool     cont = false;
         float3   phit = mk(0.f, 0.f, 0.f), cdir = mk(0.f, 0.f, 1.f), T2 = mk(0.f, 0.f, 0.f);
@@ -720,6 +737,8 @@ __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
                 a.sm[qsel][idx] = make_int4(dest + r, nee[r].type | (nee[r].light << 2), pixel, job);
             }
         }
+        pos += 128;
+        if (pos % kShadeWindow == 0) pos += (gridDim.x - 1) * kShadeWindow;
     }
     grads_end<ADJ>(a, sgrad);
 }
