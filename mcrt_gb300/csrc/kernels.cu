@@ -10,9 +10,10 @@
 //     k_extend           closest hit of the ray queue
 //     k_shade            one vertex of rayTrace (demo_pt.cpp:523-651): emission, NEE with
 //                        MIS against the environment and the area lights, continuation,
-//                        Russian roulette; continuing paths, ended paths and next-event
-//                        rays are appended to SoA queues by warp ballot / warp prefix sum
-//                        + one atomic per warp
+//                        Russian roulette, over windows of queue entries sorted by
+//                        material in shared memory; continuing paths, ended paths and
+//                        next-event rays are appended to SoA queues by warp ballot /
+//                        warp prefix sum + one atomic per warp
 //     k_connect          next-event rays: any hit (environment) or bounded closest hit
 //                        (area lights, which must hit the sampled emitter), MIS-weighted
 //   k_adjoint            path-replay adjoint (one thread per path, replayed from its seed)
