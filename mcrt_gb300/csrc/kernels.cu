@@ -490,19 +490,27 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_extend(WaveArgs a, int p)
 // k_shade sorts windows of kShadeWindow queue entries and shades them in rounds of 128.
 constexpr int kShadeRounds = 4, kShadeWindow = 128 * kShadeRounds;
 
-// Shading class of queue entry i: 0 a miss, 1-6 the hit material (light, Lambert, mirror,
-// dielectric, Phong, GGX).
+// Shading class of queue entry i: 0 a miss; else the hit material (light, Lambert, mirror,
+// dielectric, Phong, GGX) and, with kShadeSide, the side of the surface the ray arrives
+// from (by the first vertex normal): 1-12.  Entries of one class run the same code and
+// continue in similar directions.
+constexpr bool kShadeSide = true;
+
 __device__ __forceinline__ int shade_class(const WaveArgs& a, int p, int i)
 {
     const int prim = __float_as_int(a.hits[i].w);
     if (prim < 0) return 0;
-    const SceneView& S = a.jobs[__float_as_int(a.qo[p][i].w)].scene;
-    const int        t = S.materials[__float_as_int(__ldg(S.prim_shade + 3 * prim).w)].type & 0xff;
-    return t == MAT_GGX ? 6 : min(t, MAT_GLSY) + 1;
+    const SceneView& S = a.jobs[a.num_jobs == 1 ? 0 : __float_as_int(a.qo[p][i].w)].scene;
+    const float4     na = __ldg(S.prim_shade + 3 * prim);
+    const int        t = S.materials[__float_as_int(na.w)].type & 0xff;
+    const int        c = t == MAT_GGX ? 6 : min(t, MAT_GLSY) + 1;
+    if (!kShadeSide) return c;
+    const float4 d = a.qd[p][i];
+    return 2 * c - 1 + (d.x * na.x + d.y * na.y + d.z * na.z > 0.f ? 1 : 0);
 }
 
 // The block's kShadeWindow queue entries from `base` on, reordered by shading class (a
-// counting sort in shared memory; entries past n last), so that a warp runs one
+// counting sort in shared memory; entries past n last, class 15), so that a warp runs one
 // material's code with all its lanes.  s_perm receives the entries in sorted order; the
 // block then shades them in rounds of 128.  The order of the entries changes nothing a
 // path computes: finished samples go to ring slots of their own.
@@ -514,9 +522,9 @@ __device__ __forceinline__ void shade_order(const WaveArgs& a, int p, int base, 
     for (int r = 0; r < kShadeRounds; ++r)
     {
         const int i0 = base + r * 128 + threadIdx.x;
-        key[r] = i0 < n ? shade_class(a, p, i0) : 7;
+        key[r] = i0 < n ? shade_class(a, p, i0) : 15;
     }
-    if (threadIdx.x < 8) s_base[threadIdx.x] = 0;
+    if (threadIdx.x < 16) s_base[threadIdx.x] = 0;
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kShadeRounds; ++r)
@@ -528,16 +536,16 @@ __device__ __forceinline__ void shade_order(const WaveArgs& a, int p, int base, 
         off[r] = __shfl_sync(0xffffffffu, o, lead) + __popc(same & lanemask_lt());
     }
     __syncthreads();
-    if (threadIdx.x < 32)  // exclusive scan of the eight class counts
+    if (threadIdx.x < 32)  // exclusive scan of the class counts
     {
-        const int c = lane < 8 ? s_base[lane] : 0;
+        const int c = lane < 16 ? s_base[lane] : 0;
         int       incl = c;
-        for (int d = 1; d < 8; d <<= 1)
+        for (int d = 1; d < 16; d <<= 1)
         {
             const int y = __shfl_up_sync(0xffffffffu, incl, d);
             if (lane >= d) incl += y;
         }
-        if (lane < 8) s_base[lane] = incl - c;
+        if (lane < 16) s_base[lane] = incl - c;
     }
     __syncthreads();
 #pragma unroll
@@ -549,7 +557,7 @@ template <bool ADJ, int LIGHTS = 3>
 __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];
-    __shared__ int s_base[8], s_perm[kShadeWindow];
+    __shared__ int s_base[16], s_perm[kShadeWindow];
     const Grads G = grads_begin<ADJ>(a, sgrad);
     const int n = min(a.ctrl->qcount[p], static_cast<int>(a.capacity));
     const int lane = threadIdx.x & 31;
