@@ -109,7 +109,7 @@ class ClockSampler:
 # DRAM bytes per average launch of the traversal kernels on the default cfg1 frame
 # (ncu dram__bytes_read.sum + dram__bytes_write.sum over every launch of three frames,
 # warm caches; profiles/cfg1_dram_traffic.md).  Valid only for that exact configuration.
-CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 709.4e6, "k_extend": 563.1e6}
+CFG1_DRAM_BYTES_PER_LAUNCH = {"k_connect": 709.5e6, "k_extend": 563.7e6}
 
 
 # rows of the cfg0 / cfg1 frames the CPU port renders for cpu_baseline and --impl reference
