@@ -312,18 +312,21 @@ int mcrt_autotune(int32_t num_jobs, mcrt_scene* const* scenes, const mcrt_camera
                   void* stream);
 
 /* Forward render that allocates nothing (no reference counterpart: MCRT has no GPU and no
- * allocation constraints).  For callers that cannot call cudaMalloc while rendering --
- * code recording a CUDA graph (allocation is not capturable), plug-ins confined to a host
- * application's own memory pool, callers under a fixed memory budget.  Same result as
- * mcrt_render with ptr_mode = MCRT_PTR_DEVICE; rgb_out must be device memory.  It always
- * runs the WAVES schedule (params->schedule and params->path_chunk are not used).
+ * allocation constraints).  For callers that cannot call cudaMalloc or cudaFree while they
+ * render: plug-ins inside a host application that owns all device memory through its own
+ * pool and forbids allocations behind its back; render loops sharing the GPU with other
+ * streams, which cudaMalloc / cudaFree may stall by synchronising the device; processes
+ * that reserve their memory at start-up under a hard budget.  Same image as mcrt_render
+ * with ptr_mode = MCRT_PTR_DEVICE; rgb_out must be device memory.  It always runs the
+ * WAVES schedule (params->schedule and params->path_chunk are not used).
  * Scratch: one fixed file-scope device array of about 50 MB, held by every GPU that loads
  * the library's module until the process exits; at most 65,536 path slots per wave
  * (spp <= 65,536) and 65,536 waves per call, larger requests fail with
  * MCRT_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's device
- * address; make it before any stream capture.  All calls share the array: calls whose
- * work overlaps on the GPU race, so serialise them.  stats->device_ms is not measured
- * (timing would need events). */
+ * address and keeps it for the process (it does not survive cudaDeviceReset); make that
+ * first call before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU race, so serialise them.  The calling thread's current device is left
+ * as it was.  stats->device_ms is not measured (timing would need events). */
 int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera, const mcrt_render_params* params,
                         float* rgb_out_device, mcrt_render_stats* stats, void* stream);
 

@@ -22,18 +22,29 @@ from .scene import CameraDesc, GpuScene
 class _RenderFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, albedo, emission, owner):
-        owner._apply(albedo, emission)
+        params = (albedo.detach().clone(), emission.detach().clone())
+        owner._apply(*params)
         img = torch.empty((owner.camera.height, owner.camera.width, 3), dtype=torch.float32, device=albedo.device)
         owner.scene.render(owner.camera, out=img, **owner.kw)
         ctx.owner = owner
+        # the parameters this image was rendered with: the scene may hold others by the
+        # time backward runs (a second forward, an optimiser step), and the path-replay
+        # derivative depends on them (it divides by the albedo at each vertex)
+        ctx.params = params
         return img
 
     @staticmethod
     def backward(ctx, grad_img):
         o = ctx.owner
-        ga, ge, _ = o.scene.render_adjoint(o.camera, o.kw["spp"], o.kw["max_depth"], grad_img.contiguous(),
-                                           o.n_albedo, o.n_emission, rr_depth=o.kw["rr_depth"], seed=o.kw["seed"],
-                                           traverse=o.kw["traverse"])
+        current = o.applied
+        o._apply(*ctx.params)
+        try:
+            ga, ge, _ = o.scene.render_adjoint(o.camera, o.kw["spp"], o.kw["max_depth"], grad_img.contiguous(),
+                                               o.n_albedo, o.n_emission, rr_depth=o.kw["rr_depth"],
+                                               seed=o.kw["seed"], traverse=o.kw["traverse"])
+        finally:
+            if current is not None and current[0] is not ctx.params[0]:
+                o._apply(*current)  # the scene keeps the latest forward's parameters
         return ga.clone(), ge.clone(), None
 
 
@@ -50,6 +61,7 @@ class DiffRender:
         self.em_idx = np.array([mats[i].emission_param for i in self.em_mats], np.int64)
         self.n_albedo = int(self.alb_idx.max() + 1) if self.alb_idx.size else 0
         self.n_emission = int(self.em_idx.max() + 1) if self.em_idx.size else 0
+        self.applied = None  # the (albedo, emission) pair the scene's materials hold
 
     def _apply(self, albedo: torch.Tensor, emission: torch.Tensor):
         a = albedo.detach().float().cpu().numpy()
@@ -60,6 +72,7 @@ class DiffRender:
         for mi, k in zip(self.em_mats, self.em_idx):
             mats[mi].color = tuple(float(x) for x in e[k])
         self.scene.set_materials(mats)
+        self.applied = (albedo, emission)
 
     def __call__(self, albedo: torch.Tensor, emission: torch.Tensor) -> torch.Tensor:
         return _RenderFn.apply(albedo, emission, self)

@@ -1,22 +1,30 @@
-// mcrt_render_noalloc: the forward render for callers that must not allocate device
-// memory during the call -- e.g. code running while a CUDA graph is being captured
-// (cudaMalloc is not capturable), plug-ins that live inside a host application's own
-// device-memory pool or arena, or callers that run under a hard memory budget.
+// mcrt_render_noalloc: the forward render for callers that cannot call cudaMalloc (or
+// cudaFree) while they render:
+//   - plug-ins living inside a host application that owns all device memory through its
+//     own pool or arena and forbids allocations behind its back, so that its own
+//     accounting and budget stay true;
+//   - latency-bound render loops sharing the GPU with other streams: cudaMalloc and
+//     cudaFree may synchronise the device and stall every stream on it;
+//   - processes that reserve their memory at start-up under a hard budget and must not
+//     grow afterwards.
 //
 // The wavefront needs scratch memory for its queues, its per-path ring and its counters.
 // Here it lives in a file-scope static __device__ array of fixed size
-// (kNoAllocScratchBytes): no cudaMalloc, cudaFree, event, graph or library allocation
-// happens in the call.  The array belongs to this file's module, so every GPU that loads
-// it holds it until the process exits.  The render runs the wave schedule with waves of
-// at most kNoAllocPaths paths and at most kNoAllocWaves waves; requests beyond either are
-// rejected with MCRT_ERR_INVALID_ARGUMENT.
+// (kNoAllocScratchBytes, about 50 MB): no cudaMalloc, cudaFree, event, graph or library
+// allocation happens in the call.  The array belongs to this file's module, so every GPU
+// that loads it holds it until the process exits.  The render runs the wave schedule with
+// waves of at most kNoAllocPaths paths and at most kNoAllocWaves waves; requests beyond
+// either are rejected with MCRT_ERR_INVALID_ARGUMENT.
 //
 // Host code cannot use the array's name as a device address (on the host it is a
 // stand-in).  The first call on a device takes the array's device address with
-// cudaGetSymbolAddress while that device is current and caches it; make that first call
-// before any stream capture begins.  Every call shares the one array, so two calls whose
-// work overlaps on the GPU (different streams, or another host thread) race: serialise
-// them.  Everything that must start at zero is cleared at the start of each call.
+// cudaGetSymbolAddress while that device is current and caches it per device ordinal;
+// make that first call before any stream capture begins.  The cached address does not
+// survive cudaDeviceReset (the module is loaded again, possibly elsewhere): do not reset a
+// device between calls.  Every call shares the one array, so two calls whose work
+// overlaps on the GPU (different streams, or another host thread) race: serialise them.
+// Everything that must start at zero is cleared at the start of each call.  The call
+// leaves the calling thread's current device as it found it.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -42,6 +50,20 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 constexpr int kMaxDevices = 64;
 std::mutex    g_setup_mu;
 void*         g_scratch_ptr[kMaxDevices] = {};
+
+// restores the calling thread's current device on every return path
+struct CurrentDeviceGuard
+{
+    int  saved = -1;
+    CurrentDeviceGuard()
+    {
+        if (cudaGetDevice(&saved) != cudaSuccess) saved = -1;
+    }
+    ~CurrentDeviceGuard()
+    {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
 
 struct Layout
 {
@@ -113,10 +135,14 @@ extern "C" int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera,
                                  std::to_string(waves) + " waves, more than the " + std::to_string(kNoAllocWaves) +
                                  " its fixed scratch holds (at most " +
                                  std::to_string(kNoAllocWaves * per_wave) + " paths per call)");
-        cudaError_t e = cudaSetDevice(scene_device(scene));
-        if (e != cudaSuccess) return set_error(MCRT_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
-        int dev = scene_device(scene);
+        const int dev = scene_device(scene);
         if (dev < 0 || dev >= kMaxDevices) return set_error(MCRT_ERR_INVALID_ARGUMENT, "device index out of range");
+        CurrentDeviceGuard keep_device;
+        cudaError_t        e = cudaSetDevice(dev);
+        if (e != cudaSuccess) return set_error(MCRT_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+        // a launch error left by the caller's earlier work is not this call's: clear it so
+        // the check after the launches below sees only these launches
+        (void)cudaGetLastError();
         void* base = nullptr;
         {
             std::lock_guard<std::mutex> lock(g_setup_mu);

@@ -6,9 +6,8 @@ module, and only as the checker.  Two libraries live here:
 * ``oracle/_build/liborc.so``: the CPU restatement of the reference path tracer
   (``pt_oracle.cpp``), built from this directory by :func:`build_restatement`.
 * ``oracle/_ref/libmcrt_ref.so``: the reference renderer's own C++ sources compiled
-  by ``oracle/Makefile`` where they lie.  Only present where the reference sources
-  are (it is not shipped anywhere else); :func:`load_reference` returns None
-  otherwise.
+  by ``oracle/Makefile`` from the staged copy ``baseline/_ref`` (``oracle/stage_reference.py``).
+  Only present where those sources are; :func:`load_reference` returns None otherwise.
 """
 from __future__ import annotations
 
@@ -22,7 +21,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 ORC_SO = os.path.join(BUILD_DIR, "liborc.so")
 REF_SO = os.path.join(HERE, "_ref", "libmcrt_ref.so")
-REF_SOURCES = os.environ.get("MCRT_REFERENCE_DIR", "/root/reference")
 
 P = ctypes.c_void_p
 I = ctypes.c_int
@@ -44,10 +42,13 @@ def build_restatement(force: bool = False) -> str:
 
 
 def build_reference() -> str | None:
-    """Compile the reference sources into oracle/_ref when they are present here."""
-    if not os.path.isdir(os.path.join(REF_SOURCES, "src", "core")):
+    """Compile the reference sources into oracle/_ref when they are present here (staged
+    into baseline/_ref from a checkout, or already staged)."""
+    from oracle.stage_reference import stage
+    src = stage()
+    if src is None:
         return None
-    subprocess.run(["make", "-s", "-C", HERE, f"REF={REF_SOURCES}", f"-j{os.cpu_count() or 4}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, f"REF={src}", f"-j{os.cpu_count() or 4}"], check=True)
     return REF_SO
 
 
@@ -136,6 +137,11 @@ def load_reference():
         lib.ref_envmap_radiance.argtypes = [P, P, P]
         lib.ref_render_pt.restype = I
         lib.ref_render_pt.argtypes = [P, P, P, I, P, P, I, ctypes.c_char_p, P, I, I, I, I, I, I, P, P, P, P]
+        lib.ref_pt_scene_create.restype = P
+        lib.ref_pt_scene_create.argtypes = [P, P, P, I, P, P, I, ctypes.c_char_p, P, I, I]
+        lib.ref_pt_render.restype = I
+        lib.ref_pt_render.argtypes = [P, I, I, I, I, I, I, P, P, P, P]
+        lib.ref_pt_scene_destroy.argtypes = [P]
         lib.ref_cornell_export.restype = I
         lib.ref_cornell_export.argtypes = [P, P, P, P]
         lib.ref_cornell_paths.restype = I

@@ -372,15 +372,15 @@ static void render_rows(const Scene& scene, int width, int height, int spp, int 
     }
 }
 
-extern "C" int ref_render_pt(const float* verts, const float* normals, const int* mat_ids, int n_tris,
-                             const int* mat_types, const float* mat_colors, int n_mats,
-                             const char* envmap_path, const float* cam /* origin3 target3 fov */,
-                             int width, int height, int spp, int nthreads, int row_begin,
-                             int row_end, float* out_rgb, long long* n_intersect,
-                             long long* n_occluded, double* seconds)
+// A reference scene built once and rendered band by band (the timed CPU baseline): the
+// build (Scene::finalize, which runs the SplitBVH builder) stays outside the timed renders.
+extern "C" void* ref_pt_scene_create(const float* verts, const float* normals, const int* mat_ids, int n_tris,
+                                     const int* mat_types, const float* mat_colors, int n_mats,
+                                     const char* envmap_path, const float* cam /* origin3 target3 fov */,
+                                     int width, int height)
 {
-    Scene scene;
-    int   base = -1;
+    Scene* scene = new Scene();
+    int    base = -1;
     for (int m = 0; m < n_mats; ++m)
     {
         int id = todo_addMaterial(
@@ -394,20 +394,45 @@ extern "C" int ref_render_pt(const float* verts, const float* normals, const int
                                                     v3(normals + 9 * i + 3), v3(normals + 9 * i + 6))
                                    : TriangleObject(v3(p), v3(p + 3), v3(p + 6));
         t.setMaterialID(base + mat_ids[i]);
-        scene.add(t);
+        scene->add(t);
     }
-    scene.setCamera(v3(cam), v3(cam + 3), width, height, cam[6]);
-    if (envmap_path && envmap_path[0]) scene.setEnvmap(std::string(envmap_path));
-    scene.finalize();
+    scene->setCamera(v3(cam), v3(cam + 3), width, height, cam[6]);
+    if (envmap_path && envmap_path[0]) scene->setEnvmap(std::string(envmap_path));
+    scene->finalize();
+    return scene;
+}
 
-    long long i0 = g_num_intersect.load(), o0 = g_num_occluded.load();
-    auto      t0 = std::chrono::steady_clock::now();
+// rows [row_begin, row_end) of the scene's camera frame; rays counted by the link-time
+// wrappers around SceneBVH::intersect / occluded
+extern "C" int ref_pt_render(void* h, int width, int height, int spp, int nthreads, int row_begin, int row_end,
+                             float* out_rgb, long long* n_intersect, long long* n_occluded, double* seconds)
+{
+    const Scene& scene = *static_cast<Scene*>(h);
+    long long    i0 = g_num_intersect.load(), o0 = g_num_occluded.load();
+    auto         t0 = std::chrono::steady_clock::now();
     render_rows(scene, width, height, spp, nthreads, row_begin, row_end, out_rgb);
     auto t1 = std::chrono::steady_clock::now();
     if (n_intersect) *n_intersect = g_num_intersect.load() - i0;
     if (n_occluded) *n_occluded = g_num_occluded.load() - o0;
     if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
     return 0;
+}
+
+extern "C" void ref_pt_scene_destroy(void* h) { delete static_cast<Scene*>(h); }
+
+extern "C" int ref_render_pt(const float* verts, const float* normals, const int* mat_ids, int n_tris,
+                             const int* mat_types, const float* mat_colors, int n_mats,
+                             const char* envmap_path, const float* cam /* origin3 target3 fov */,
+                             int width, int height, int spp, int nthreads, int row_begin,
+                             int row_end, float* out_rgb, long long* n_intersect,
+                             long long* n_occluded, double* seconds)
+{
+    void* h = ref_pt_scene_create(verts, normals, mat_ids, n_tris, mat_types, mat_colors, n_mats, envmap_path, cam,
+                                  width, height);
+    int rc = ref_pt_render(h, width, height, spp, nthreads, row_begin, row_end, out_rgb, n_intersect, n_occluded,
+                           seconds);
+    ref_pt_scene_destroy(h);
+    return rc;
 }
 
 // Per-sample radiance of demo_pt's rayTrace on its own Cornell box, single-threaded in

@@ -13,7 +13,8 @@ specifies it (`OracleScene(..., 32)`), on the same rows, at the configuration's 
 Russian-roulette setting.  Both run OpenMP over pixels on the same number of threads.
 
 This is test infrastructure: it needs `oracle/_ref`, which is built only where the
-reference sources are present, so it runs on the development host, not on the GPU machine.
+reference sources are present (a checkout, or the staged copy in `baseline/_ref`).
+`bench.py --impl reference` uses `ReferenceTracer` for its timed CPU baseline.
 
     python -m oracle.time_reference --workload cfg1 --rows 448 480 --spp 16
 """
@@ -42,32 +43,52 @@ def reference_materials(desc):
     return types, colors
 
 
-def time_reference(desc, cam, spp, rows, threads):
-    lib = load_reference()
-    if lib is None:
-        raise SystemExit("oracle/_ref is not built here (the reference sources are absent)")
-    v = np.ascontiguousarray(desc.vertices, np.float32)
-    n = None if desc.normals is None else np.ascontiguousarray(desc.normals, np.float32)
-    mid = np.ascontiguousarray(desc.material_ids, np.int32)
-    types, colors = reference_materials(desc)
-    c7 = np.array(list(cam.origin) + list(cam.target) + [cam.fov_y], np.float32)
-    out = np.zeros((cam.height, cam.width, 3), np.float32)
-    ni, no, sec = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_double(0.0)
-    with tempfile.TemporaryDirectory() as tmp:
-        env_path = b""
-        if desc.envmap is not None:
-            p = os.path.join(tmp, "env.bin")
-            scenes.write_envmap_bin(p, desc.envmap)
-            env_path = p.encode()
+class ReferenceTracer:
+    """demo_pt.cpp's own rayTrace over a scene built through the reference API (the
+    SplitBVH build runs here, once); render() times a band of rows."""
+
+    def __init__(self, desc, cam):
+        lib = load_reference()
+        if lib is None:
+            raise RuntimeError("oracle/_ref is not built here (the reference sources are absent)")
+        self.lib, self.cam = lib, cam
+        v = np.ascontiguousarray(desc.vertices, np.float32)
+        n = None if desc.normals is None else np.ascontiguousarray(desc.normals, np.float32)
+        mid = np.ascontiguousarray(desc.material_ids, np.int32)
+        types, colors = reference_materials(desc)
+        c7 = np.array(list(cam.origin) + list(cam.target) + [cam.fov_y], np.float32)
         t0 = time.perf_counter()
-        lib.ref_render_pt(ptr(v), ptr(n), ptr(mid), len(mid), ptr(types), ptr(colors), len(types), env_path,
-                          ptr(c7), cam.width, cam.height, spp, threads, rows[0], rows[1], ptr(out),
-                          ctypes.byref(ni), ctypes.byref(no), ctypes.byref(sec))
-        total = time.perf_counter() - t0
-    rays = ni.value + no.value
-    return {"rays": rays, "render_s": round(sec.value, 3), "scene_build_s": round(total - sec.value, 2),
-            "mrays_per_s": round(rays / sec.value / 1e6, 3),
-            "image_mean": float(out[rows[0]:rows[1]].mean())}
+        with tempfile.TemporaryDirectory() as tmp:
+            env_path = b""
+            if desc.envmap is not None:
+                p = os.path.join(tmp, "env.bin")
+                scenes.write_envmap_bin(p, desc.envmap)
+                env_path = p.encode()
+            self.h = lib.ref_pt_scene_create(ptr(v), ptr(n), ptr(mid), len(mid), ptr(types), ptr(colors),
+                                             len(types), env_path, ptr(c7), cam.width, cam.height)
+        self.build_s = time.perf_counter() - t0
+        self.out = np.zeros((cam.height, cam.width, 3), np.float32)
+
+    def render(self, spp, rows, threads):
+        ni, no, sec = ctypes.c_longlong(0), ctypes.c_longlong(0), ctypes.c_double(0.0)
+        self.lib.ref_pt_render(self.h, self.cam.width, self.cam.height, spp, threads, rows[0], rows[1],
+                               ptr(self.out), ctypes.byref(ni), ctypes.byref(no), ctypes.byref(sec))
+        return {"rays": ni.value + no.value, "seconds": sec.value, "band": self.out[rows[0]:rows[1]]}
+
+    def close(self):
+        if self.h:
+            self.lib.ref_pt_scene_destroy(self.h)
+            self.h = None
+
+
+def time_reference(desc, cam, spp, rows, threads):
+    tr = ReferenceTracer(desc, cam)
+    try:
+        r = tr.render(spp, rows, threads)
+    finally:
+        tr.close()
+    return {"rays": r["rays"], "render_s": round(r["seconds"], 3), "scene_build_s": round(tr.build_s, 2),
+            "mrays_per_s": round(r["rays"] / r["seconds"] / 1e6, 3), "image_mean": float(r["band"].mean())}
 
 
 def time_port(desc, cam, spp, max_depth, rr_depth, rows, threads):

@@ -18,6 +18,13 @@ Fixtures (all seeded):
                            on its own Cornell box: per-pixel means of independent batches
   ref_paths_cornell.npz    the same path tracer single-threaded from the start of its global
                            random stream: every sample's radiance, for a draw-by-draw replay
+  ref_traverse_cfg1.npz    hit parity at full scale: the displaced level-8 icosphere + ground
+                           (1,310,722 T, scenes.cfg1_scene(); only its SHA-256 is stored, the
+                           triangles are regenerated where the test runs), 65,536 rays in each
+                           of the primary / bounce / incoherent / segment classes and the
+                           reference SplitBVH's closest hits (prim, t) and occluded answers.
+                           Its reference tree takes about 60-110 s to build:
+                               python tests/golden/make_golden.py --only-cfg1
 """
 from __future__ import annotations
 
@@ -151,6 +158,58 @@ def traverse_fixture(ref, name, desc_verts, normals, cam, rng, n_random=8192, ra
         print(f"{name}/{k}: {r.shape[0]} rays, hit {np.mean(p >= 0):.3f}")
     ref.ref_bvh_destroy(h)
     np.savez_compressed(os.path.join(OUT, f"ref_traverse_{name}.npz"), **out)
+
+
+def geometry_sha256(verts) -> str:
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(verts, np.float32).tobytes()).hexdigest()
+
+
+def cfg1_traverse_fixture(ref, n=65536, seed=20261204):
+    """Hit parity on the 1.31 M-triangle geometry of the large configuration, where the
+    reference's absolute |det| < 1e-6 cull bites (edges of ~4.7e-3 on a unit sphere)."""
+    rng = np.random.default_rng(seed)
+    desc = scenes.cfg1_scene()
+    verts = np.ascontiguousarray(desc.vertices, np.float32)
+    h, _ = ref_tree(ref, verts)  # the tree itself is not stored (about 100 MB)
+    sets = {}
+    # primary: the large configuration's camera at random film positions
+    cam = scenes.cfg1_camera(1024, 1024).as_array()
+    m = rng.uniform(0, 1, (n, 2)).astype(np.float32)
+    o, d = np.zeros(3, np.float32), np.zeros(3, np.float32)
+    po, pd = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+    for i in range(n):
+        ref.ref_camera_ray(ptr(cam[0:3]), ptr(cam[3:6]), 1024, 1024, float(cam[9]), float(m[i, 0]),
+                           float(m[i, 1]), ptr(o), ptr(d))
+        po[i], pd[i] = o, d
+    sets["primary"] = make_rays(po, pd)
+    t, p, _, _ = ref_hits(ref, h, sets["primary"])
+    hit = np.nonzero(p >= 0)[0]
+    # bounce: cosine-distributed about the interpolated normal (flipped to the viewer) at
+    # primary hit points, resampled to n rays
+    pick = rng.choice(hit, n)
+    ph = (po[pick] + pd[pick] * t[pick, None]).astype(np.float32)
+    nrm = unit(desc.normals.reshape(-1, 3, 3)[p[pick]].mean(axis=1))
+    flip = np.sign(np.sum(-pd[pick] * nrm, axis=1, keepdims=True))
+    flip[flip == 0] = 1
+    nrm = nrm * flip
+    sets["bounce"] = make_rays(ph, unit(nrm + unit(rng.normal(size=nrm.shape))))
+    # incoherent: origins uniform in [-2, 2]^3, directions uniform on the sphere (the
+    # random-ray measurement of the reference SplitBVH)
+    sets["incoherent"] = make_rays(rng.uniform(-2, 2, (n, 3)).astype(np.float32), unit(rng.normal(size=(n, 3))))
+    # segment: finite rays between random points around the sphere (next-event-like)
+    o2 = rng.uniform(-1.3, 1.3, (n, 3)).astype(np.float32)
+    seg = rng.uniform(-1.3, 1.3, (n, 3)).astype(np.float32) - o2
+    sets["segment"] = make_rays(o2, unit(seg), tmax=np.linalg.norm(seg, axis=1).astype(np.float32))
+    out = dict(verts_sha256=np.array(geometry_sha256(verts)), num_triangles=np.array(verts.shape[0]))
+    for k, r in sets.items():
+        t, p, _, _ = ref_hits(ref, h, r)
+        out[f"rays_{k}"], out[f"t_{k}"], out[f"prim_{k}"] = r, t, p
+        tfar = np.where(np.isfinite(r[:, 7]), r[:, 7], np.inf).astype(np.float32)
+        out[f"occ_{k}"] = ref_occluded(ref, h, r, tfar).astype(np.int8)
+        print(f"cfg1/{k}: {r.shape[0]} rays, hit {np.mean(p >= 0):.3f}")
+    ref.ref_bvh_destroy(h)
+    np.savez_compressed(os.path.join(OUT, "ref_traverse_cfg1.npz"), **out)
 
 
 def functions_fixture(ref, rng):
@@ -366,6 +425,9 @@ def main():
         return
     if "--only-consistent" in sys.argv:
         consistent_fixture(ref)
+        return
+    if "--only-cfg1" in sys.argv:
+        cfg1_traverse_fixture(ref)
         return
     film_fixture(ref)
     consistent_fixture(ref)

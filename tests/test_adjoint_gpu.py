@@ -93,6 +93,31 @@ def test_torch_autograd_function(cuda_device):
     np.testing.assert_allclose(e.grad.cpu().numpy(), ge.cpu().numpy(), rtol=1e-4, atol=1e-6)
 
 
+def test_torch_autograd_backward_uses_its_own_forward_parameters(cuda_device):
+    """forward(a1), forward(a2), then backward of the first: the gradient is the adjoint at
+    a1 (the scene holds a2 when that backward runs), and the scene keeps a2 afterwards."""
+    import torch
+    from mcrt_gb300 import scenes
+    from mcrt_gb300.autograd import DiffRender
+    desc, cam, albedo, emission, sc = _setup()
+    r = DiffRender(sc, cam, spp=8, max_depth=DEPTH, seed=2)
+    a1 = torch.tensor(albedo, device=cuda_device, requires_grad=True)
+    e1 = torch.tensor(emission, device=cuda_device, requires_grad=True)
+    a2 = torch.tensor(np.clip(albedo * 0.6 + 0.2, 0.05, 0.95), device=cuda_device, requires_grad=True)
+    e2 = torch.tensor(emission * 1.5, device=cuda_device, requires_grad=True)
+    img1 = r(a1, e1)
+    img2 = r(a2, e2)
+    w = torch.randn_like(img1)
+    (img1 * w).sum().backward()
+    # the scene was put back to the second forward's parameters after that backward
+    after, _ = sc.render(cam, spp=8, max_depth=DEPTH, seed=2)
+    np.testing.assert_array_equal(after, img2.detach().cpu().numpy())
+    sc.set_materials(scenes.cfg3_with_params(albedo, emission).materials)
+    ga, ge, _ = sc.render_adjoint(cam, 8, DEPTH, w, albedo.shape[0], 1, seed=2)
+    np.testing.assert_allclose(a1.grad.cpu().numpy(), ga.cpu().numpy(), rtol=1e-4, atol=1e-6)
+    np.testing.assert_allclose(e1.grad.cpu().numpy(), ge.cpu().numpy(), rtol=1e-4, atol=1e-6)
+
+
 def test_adjoint_forward_time_ratio(cuda_device):
     """Forward + adjoint stays within 3x the forward time (same image, same spp)."""
     import time

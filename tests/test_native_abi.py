@@ -93,8 +93,9 @@ def test_scenebvh_adapter_compiles_against_reference_headers(tmp_path):
     links against the library (where the reference sources are present)."""
     import subprocess
     import pytest
-    ref = os.environ.get("MCRT_REFERENCE_DIR", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src", "core")):
+    from oracle.stage_reference import stage
+    ref = stage()
+    if ref is None:
         pytest.skip("reference sources not present on this machine")
     src = os.path.join(ROOT, "mcrt_gb300", "integration", "scenebvh_gb300.cpp")
     obj = tmp_path / "scenebvh_gb300.o"

@@ -135,3 +135,105 @@ def test_l2_read_probe(cuda_device):
     g = ctypes.c_float(0.0)
     N.check(lib.mcrt_probe_l2_read(48 << 20, 20, ctypes.byref(g), None), "mcrt_probe_l2_read")
     assert 3000.0 < g.value < 100000.0, g.value
+
+
+def _chain_tree(n):
+    """A chain-shaped binary tree over n triangles: inner node i holds triangle i's leaf on
+    the left and inner node i + 1 on the right, so the tree is n - 1 levels deep."""
+    v = np.zeros((n, 3, 3), np.float32)
+    x = np.arange(n, dtype=np.float32)
+    v[:, 0, 0], v[:, 1, 0], v[:, 2, 0] = x, x + 0.5, x
+    v[:, 1, 1], v[:, 2, 2] = 0.5, 0.5
+    lo, hi = v.min(axis=1), v.max(axis=1)
+    inner, leaves = n - 1, n
+    node_box = np.zeros((inner + leaves, 6), np.float32)
+    node_info = np.zeros((inner + leaves, 6), np.int32)
+    for i in range(inner):
+        right = i + 1 if i + 1 < inner else inner + n - 1
+        node_box[i] = np.concatenate([lo[i:].min(axis=0), hi[i:].max(axis=0)])
+        node_info[i] = (0, inner + i, right, 0, 0, 0)
+    for k in range(leaves):
+        node_box[inner + k] = np.concatenate([lo[k], hi[k]])
+        node_info[inner + k] = (1, -1, -1, 0, k, 1)
+    tree = dict(node_box=node_box.ravel(), node_info=node_info.ravel(), ref_prim=np.arange(n, dtype=np.int32),
+                ref_box=np.concatenate([lo, hi], axis=1).ravel())
+    return v, tree
+
+
+def test_tree_deeper_than_the_stack_is_refused_before_any_launch(cuda_device):
+    """An external tree deeper than the 64-entry traversal stack: trace and render calls fail
+    on the host with MCRT_ERR_STACK_OVERFLOW before any kernel is launched, and the scene is
+    destroyed cleanly."""
+    from mcrt_gb300 import GpuScene, scenes
+    from mcrt_gb300 import _native as N
+    from mcrt_gb300.scene import DIFF, Material, SceneDesc
+    v, tree = _chain_tree(80)
+    sc = GpuScene(SceneDesc(v, np.zeros(80, np.int32), [Material(DIFF)]), builder="external", external_tree=tree)
+    rays = np.zeros((4, 8), np.float32)
+    rays[:, 0:3] = (0.25, 0.1, -1.0)
+    rays[:, 3] = 1e-4
+    rays[:, 6] = 1.0
+    rays[:, 7] = np.inf
+    for call in (lambda: sc.trace_closest(rays), lambda: sc.trace_any(rays),
+                 lambda: sc.render(scenes.cfg0_camera(8, 8), spp=1, max_depth=2)):
+        with pytest.raises(N.McrtError) as e:
+            call()
+        assert "stack overflow" in str(e.value) and "deeper" in str(e.value), str(e.value)
+    sc.close()
+
+
+@pytest.fixture(scope="module")
+def cfg1_hits():
+    """The 1.31 M-triangle geometry of the large configuration (regenerated here and checked
+    against the fixture's SHA-256) with the reference SplitBVH's answers."""
+    import hashlib
+    from mcrt_gb300 import GpuScene, scenes
+    fx = golden("ref_traverse_cfg1.npz")
+    desc = scenes.cfg1_scene()
+    verts = np.ascontiguousarray(desc.vertices, np.float32)
+    assert hashlib.sha256(verts.tobytes()).hexdigest() == str(fx["verts_sha256"]), "cfg1 geometry differs"
+    return fx, verts, GpuScene(desc)
+
+
+CFG1_SETS = ["primary", "bounce", "incoherent", "segment"]
+
+
+def test_fast_mode_nonmarginal_at_1_3m_triangles(cfg1_hits, cuda_device):
+    """The hit contract at full scale: on the library's own tree of the 1,310,722-triangle
+    scene, the watertight traversal returns the reference SplitBVH's prim with t within 4 ulp
+    on every non-marginal ray, 65,536 rays per class.  At this scale the reference's absolute
+    |det| < 1e-6 cull rejects grazing hits on the ~4.7e-3 edges, and the FAST test applies
+    the same cull."""
+    from mcrt_gb300 import TRAVERSE_FAST
+    fx, verts, sc = cfg1_hits
+    report = {}
+    for k in CFG1_SETS:
+        rays = fx[f"rays_{k}"]
+        out = sc.trace_closest(rays, TRAVERSE_FAST)
+        bad, marginal = classify(verts, rays, fx[f"t_{k}"], fx[f"prim_{k}"], out[:, 0], out[:, 3].view(np.int32))
+        assert not bad.any(), f"cfg1/{k}: {bad.sum()} non-marginal mismatches, e.g. ray {np.argmax(bad)}"
+        report[k] = int(marginal.sum())
+        assert marginal.sum() <= rays.shape[0] // 200, f"cfg1/{k}: {marginal.sum()} marginal disagreements"
+    print("marginal disagreements per 65,536 rays:", report)
+
+
+def test_fast_any_hit_matches_occluded_at_1_3m_triangles(cfg1_hits, cuda_device):
+    """SceneBVH::occluded(ray, tfar) on the full-scale scene: the any-hit traversal over
+    [1e-4, tfar - 1e-4] agrees with the reference except on rays whose reference closest hit
+    is marginal or lies within 4 ulp of the bound."""
+    from mcrt_gb300 import TRAVERSE_FAST
+    from parity import ulp_diff
+    fx, verts, sc = cfg1_hits
+    for k in CFG1_SETS:
+        rays = fx[f"rays_{k}"].copy()
+        rays[:, 3] = np.float32(1e-4)
+        rays[:, 7] = (rays[:, 7] - np.float32(1e-4)).astype(np.float32)
+        occ = sc.trace_any(rays, TRAVERSE_FAST)
+        diff = occ != fx[f"occ_{k}"].astype(np.int32)
+        if diff.any():
+            got = sc.trace_closest(fx[f"rays_{k}"], TRAVERSE_FAST)
+            _, marginal = classify(verts, fx[f"rays_{k}"], fx[f"t_{k}"], fx[f"prim_{k}"], got[:, 0],
+                                   got[:, 3].view(np.int32))
+            near_bound = (fx[f"prim_{k}"] >= 0) & (ulp_diff(fx[f"t_{k}"], rays[:, 7]) <= 4)
+            unexplained = diff & ~marginal & ~near_bound
+            assert unexplained.sum() <= max(2, rays.shape[0] // 5000), f"cfg1/{k}: {unexplained.sum()} of {diff.sum()}"
