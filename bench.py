@@ -111,9 +111,10 @@ class ClockSampler:
 
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per extension ray of
 # k_extend on the large configuration, from a capture of three full-queue launches of a
-# reduced case (2,097,152-ray queue, same scene and frame); the bench scales it by the
-# extension rays of an average launch of the measured configuration.
-K_EXTEND_DRAM_BYTES_PER_RAY = None
+# reduced case (2,097,152-ray queue, same scene and frame: 337.9 MB per launch); the bench
+# scales it by the extension rays of an average launch of the measured configuration.  An
+# upper bound for larger launches, whose rays share more of the tree lines fetched.
+K_EXTEND_DRAM_BYTES_PER_RAY = 161.1
 
 
 # rows of the cfg0 / cfg1 frames the CPU port renders for cpu_baseline and --impl reference
@@ -607,8 +608,9 @@ def main():
                          "limiter": "dependent-load latency and SIMT divergence (ncu: long-scoreboard stalls, "
                                     "about 10 of 32 lanes active per instruction)",
                          "traffic": None if traffic is None else int(traffic),
-                         "traffic_unit": "DRAM bytes per launch (ncu read + write of a reduced case, per "
-                                         "extension ray, times this configuration's rays per launch)",
+                         "traffic_unit": "DRAM bytes per launch: ncu read + write per extension ray of a "
+                                         "2 M-ray-queue case (161.1 B) times this configuration's rays per launch "
+                                         "(an upper bound: larger launches share more tree lines)",
                          "algorithmic_bytes_per_launch": int(per_launch_bytes),
                          "avg_launch_ms": round(avg_launch_ms, 4),
                          "hbm": {"peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),

@@ -220,6 +220,23 @@ int mcrt_vertex_alpha(const float* vertices, const float* normals, int64_t num_t
 int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int32_t leaf_size, int32_t* num_nodes,
                    int32_t* num_refs, float* node_box, int32_t* node_info, int32_t* ref_prim, float* ref_box);
 
+/* Scene inputs from the reference's file formats (host only, no GPU needed).
+ * mcrt_mesh_load_obj: the triangles Scene::loadModel(path, transform, mat) adds
+ *   (scene.cpp:368-408): the OBJ read as Mesh::Mesh(filepath) does (mesh.cpp:24-60: "v"
+ *   and "f" records, 1-based indices, the first three of a face), every vertex multiplied
+ *   by `transform` (16 floats, column-major like glm::mat4; NULL = identity), then
+ *   Mesh::genNormals (mesh.cpp:66-116): per-vertex normals and consistent-normal alphas.
+ *   Call with vertices == NULL to get *num_triangles; then with arrays of that many
+ *   triangles: vertices / normals [n][3][3] (a, b, c), vertex_alpha [n][3] (normals and
+ *   vertex_alpha may be NULL) -- the mcrt_scene_desc fields of the same names.
+ * mcrt_envmap_load_bin: the environment map file EnvmapLoader reads (envmap.cpp:98-119):
+ *   {int32 width, int32 height} then width * height RGB floats, top row first.  Call with
+ *   rgb == NULL to get the size; then with rgb [height][width][3] and the same size (the
+ *   mcrt_scene_desc env_rgb layout). */
+int mcrt_mesh_load_obj(const char* path, const float* transform, int64_t* num_triangles, float* vertices,
+                       float* normals, float* vertex_alpha);
+int mcrt_envmap_load_bin(const char* path, int32_t* width, int32_t* height, float* rgb);
+
 /* Scene cache files (no reference counterpart: the reference rebuilds its SplitBVH, 58 s
  * at 1.3 M triangles, on every run).  mcrt_scene_save writes the prepared device scene
  * (node layouts, leaf triangles, shading, emitter and environment tables) with the hash of

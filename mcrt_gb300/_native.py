@@ -122,6 +122,9 @@ EXPORTS = {
     "mcrt_build_bvh": (c_int32, [c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), ctypes.POINTER(c_int32),
                                  c_void_p, c_void_p, c_void_p, c_void_p]),
     "mcrt_scene_desc_hash": (c_int32, [ctypes.POINTER(SceneDesc), ctypes.POINTER(ctypes.c_uint64)]),
+    "mcrt_mesh_load_obj": (c_int32, [ctypes.c_char_p, c_void_p, ctypes.POINTER(c_int64), c_void_p, c_void_p,
+                                     c_void_p]),
+    "mcrt_envmap_load_bin": (c_int32, [ctypes.c_char_p, ctypes.POINTER(c_int32), ctypes.POINTER(c_int32), c_void_p]),
     "mcrt_scene_save": (c_int32, [c_void_p, ctypes.c_char_p]),
     "mcrt_scene_load": (c_int32, [ctypes.c_char_p, ctypes.c_uint64, ctypes.POINTER(c_void_p)]),
     "mcrt_film_encode": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int64, ctypes.POINTER(c_int64),

@@ -25,6 +25,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/mcrt_gb300.h"
@@ -1059,7 +1060,9 @@ struct mcrt_scene
     MaterialGPU*       d_materials = nullptr;
     std::vector<int64_t> array_bytes;  // bytes of each uploaded array, in upload order
     uint64_t             desc_hash = 0;  // of the description the scene was built from
-    int*               d_err = nullptr;
+    // error word of the batch-trace calls, one per CUDA stream: calls on one stream run in
+    // order, and calls on different streams (from different host threads) do not share one
+    std::unordered_map<void*, int*> err_by_stream;
     std::mutex         mu;
 };
 
@@ -2092,6 +2095,7 @@ int mcrt_scene_destroy(mcrt_scene* s)
     if (!s) return MCRT_OK;
     cudaSetDevice(s->device);
     for (void* p : s->allocs) cudaFree(p);
+    for (auto& e : s->err_by_stream) cudaFree(e.second);
     delete s;
     return MCRT_OK;
 }
@@ -2178,8 +2182,25 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
         d_rays = static_cast<const float4*>(tmp_rays);
         d_out = tmp_out;
     }
-    if (!s->d_err) CK(cudaMalloc(&s->d_err, sizeof(int)));
-    CK(cudaMemsetAsync(s->d_err, 0, sizeof(int), st));
+    int* d_err = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        int*&                       slot = s->err_by_stream[stream];
+        if (!slot)
+        {
+            cudaError_t e = cudaMalloc(&slot, sizeof(int));
+            if (e != cudaSuccess)
+            {
+                slot = nullptr;
+                s->err_by_stream.erase(stream);
+                cudaFree(tmp_rays);
+                cudaFree(tmp_out);
+                return fail(MCRT_ERR_OUT_OF_MEMORY, "trace error word allocation failed");
+            }
+        }
+        d_err = slot;
+    }
+    CK(cudaMemsetAsync(d_err, 0, sizeof(int), st));
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<false, 0>, kTraceBlock, 0);
     int64_t want = (n + kTraceBlock - 1) / kTraceBlock;
@@ -2189,21 +2210,21 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
     if (any)
     {
         if (traverse == MCRT_TRAVERSE_REF)
-            k_trace<true, 1><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, nullptr, o, s->d_err);
+            k_trace<true, 1><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, nullptr, o, d_err);
         else
-            k_trace<true, 0><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, nullptr, o, s->d_err);
+            k_trace<true, 0><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, nullptr, o, d_err);
     }
     else
     {
         if (traverse == MCRT_TRAVERSE_REF)
-            k_trace<false, 1><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, hits, nullptr, s->d_err);
+            k_trace<false, 1><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, hits, nullptr, d_err);
         else
-            k_trace<false, 0><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, hits, nullptr, s->d_err);
+            k_trace<false, 0><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, hits, nullptr, d_err);
     }
     CK(cudaGetLastError());
     int herr = 0;
     if (ptr_mode != MCRT_PTR_DEVICE) CK(cudaMemcpyAsync(out, tmp_out, out_bytes, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&herr, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     cudaFree(tmp_rays);
     cudaFree(tmp_out);

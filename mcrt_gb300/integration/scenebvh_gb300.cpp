@@ -11,7 +11,11 @@
 //   * occluded(ray, tfar): a hit with NUM_EPS_RAY < t < tfar - NUM_EPS_RAY;
 //   * hits are bit-identical to the SplitBVH backend when the reference tree is passed in
 //     (MCRT_BUILD_EXTERNAL + MCRT_TRAVERSE_REF); with the library's own tree and the
-//     watertight traversal (the defaults below) they agree on every non-marginal ray.
+//     watertight traversal (the default) they agree on every non-marginal ray.
+// The environment variable MCRT_SCENEBVH_TREE=splitbvh selects the first: the adapter then
+// builds the reference's own SplitBVH (through the public static SplitBVH::build, over
+// the same BoundedTriangle references SplitBVH::SplitBVH makes, splitbvh.cpp:1410-1433),
+// hands its nodes to the library and traverses in the reference's order and arithmetic.
 // The reference has no error channel; a failed call prints mcrt_last_error() and aborts,
 // as the reference's builder does on its own failures (splitbvh.cpp:1556, 1596).
 //
@@ -19,8 +23,12 @@
 // mcrt_trace_any on batches, or replace DemoSimple::run with mcrt_render.
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <memory>
 #include <vector>
 
+#include "acceleration/splitbvh.h"
+#include "boundedtriangle.h"
 #include "constants.h"
 #include "intersection.h"
 #include "mcrt_gb300.h"
@@ -33,7 +41,52 @@ namespace {
 struct Gb300Context
 {
     mcrt_scene* scene = nullptr;
+    int32_t     traverse = MCRT_TRAVERSE_FAST;
 };
+
+// The reference tree in the form of mcrt_bvh_tree: nodes depth-first, leaf references with
+// their clipped bounds (SplitBVHBranchNode / SplitBVHLeafNode, splitbvh.h:32-58).
+struct TreeDump
+{
+    std::vector<float>   node_box, ref_box;
+    std::vector<int32_t> node_info, ref_prim;
+
+    int add(const SplitBVHNode* n)
+    {
+        const int   idx = static_cast<int>(node_info.size() / 6);
+        const AABB& b = *n->bounding_box;
+        for (int k = 0; k < 3; ++k) node_box.push_back(b.min()[k]);
+        for (int k = 0; k < 3; ++k) node_box.push_back(b.max()[k]);
+        node_info.resize(node_info.size() + 6, 0);
+        if (const SplitBVHLeafNode* leaf = dynamic_cast<const SplitBVHLeafNode*>(n))
+        {
+            const int begin = static_cast<int>(ref_prim.size());
+            for (int i = 0; i < k_sbvh_leaf_node_size; ++i)
+            {
+                if (!leaf->primitive[i]) continue;
+                ref_prim.push_back(leaf->primitive[i]->originalTriangle()->primitiveID());
+                const AABB& c = leaf->primitive[i]->clippedBoundingBox();
+                for (int k = 0; k < 3; ++k) ref_box.push_back(c.min()[k]);
+                for (int k = 0; k < 3; ++k) ref_box.push_back(c.max()[k]);
+            }
+            const int32_t v[6] = {1, -1, -1, 0, begin, static_cast<int32_t>(ref_prim.size()) - begin};
+            std::memcpy(&node_info[6 * idx], v, sizeof(v));
+            return idx;
+        }
+        const SplitBVHBranchNode* br = static_cast<const SplitBVHBranchNode*>(n);
+        const int                 l = add(br->left_child.get());
+        const int                 r = add(br->right_child.get());
+        const int32_t             v[6] = {0, l, r, static_cast<int32_t>(br->split_axis), 0, 0};
+        std::memcpy(&node_info[6 * idx], v, sizeof(v));
+        return idx;
+    }
+};
+
+bool use_reference_tree()
+{
+    const char* e = std::getenv("MCRT_SCENEBVH_TREE");
+    return e && std::strcmp(e, "splitbvh") == 0;
+}
 
 void check(int rc, const char* what)
 {
@@ -76,6 +129,33 @@ SceneBVH::SceneBVH(const std::vector<TriangleObject>& triangles) : m_triangles_r
     d.materials = &m;
     d.builder = MCRT_BUILD_SAH;
     Gb300Context* ctx = new Gb300Context;
+    TreeDump      dump;
+    mcrt_bvh_tree tree = {};
+    if (use_reference_tree() && n > 0)
+    {
+        std::vector<std::shared_ptr<Triangle> >        owned;
+        std::vector<std::shared_ptr<BoundedTriangle> > refs;
+        owned.reserve(n);
+        refs.reserve(n);
+        for (size_t i = 0; i < n; ++i)
+        {
+            auto t = std::make_shared<Triangle>(triangles[i]);
+            t->setPrimitiveID(static_cast<int>(i));
+            owned.push_back(t);
+            refs.push_back(std::make_shared<BoundedTriangle>(t, t->boundingBox()));
+        }
+        std::shared_ptr<SplitBVHNode> root = SplitBVH::build(refs, 0u, "root");
+        dump.add(root.get());
+        tree.num_nodes = static_cast<int32_t>(dump.node_info.size() / 6);
+        tree.num_refs = static_cast<int32_t>(dump.ref_prim.size());
+        tree.node_box = dump.node_box.data();
+        tree.node_info = dump.node_info.data();
+        tree.ref_prim = dump.ref_prim.data();
+        tree.ref_box = dump.ref_box.data();
+        d.builder = MCRT_BUILD_EXTERNAL;
+        d.external_tree = &tree;
+        ctx->traverse = MCRT_TRAVERSE_REF;
+    }
     check(mcrt_scene_create(&d, &ctx->scene), "mcrt_scene_create");
     m_ctx = ctx;
 }
@@ -93,7 +173,7 @@ HitInfo SceneBVH::intersect(const Ray& ray) const
     mcrt_ray      r = {{ray.orig.x, ray.orig.y, ray.orig.z}, NUM_EPS_RAY, {ray.dir.x, ray.dir.y, ray.dir.z},
                        NUM_INFINITY};
     mcrt_hit      h;
-    check(mcrt_trace_closest(ctx->scene, &r, 1, &h, MCRT_TRAVERSE_FAST, MCRT_PTR_HOST, nullptr), "mcrt_trace_closest");
+    check(mcrt_trace_closest(ctx->scene, &r, 1, &h, ctx->traverse, MCRT_PTR_HOST, nullptr), "mcrt_trace_closest");
     if (h.prim < 0)
     {
         HitInfo miss;
@@ -113,6 +193,6 @@ bool SceneBVH::occluded(const Ray& ray, float tfar) const
     mcrt_ray      r = {{ray.orig.x, ray.orig.y, ray.orig.z}, NUM_EPS_RAY, {ray.dir.x, ray.dir.y, ray.dir.z},
                        tfar - NUM_EPS_RAY};
     int32_t       occ = 0;
-    check(mcrt_trace_any(ctx->scene, &r, 1, &occ, MCRT_TRAVERSE_FAST, MCRT_PTR_HOST, nullptr), "mcrt_trace_any");
+    check(mcrt_trace_any(ctx->scene, &r, 1, &occ, ctx->traverse, MCRT_PTR_HOST, nullptr), "mcrt_trace_any");
     return occ != 0;
 }

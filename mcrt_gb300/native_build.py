@@ -21,7 +21,7 @@ LIB = os.path.join(LIB_DIR, "libmcrt_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["kernels.cu", "noalloc.cu", "film.cu", "probe.cu"]
-CPP_SOURCES = ["bvh_build.cpp", "flatten.cpp", "scene_prep.cpp", "autotune.cpp", "scene_cache.cpp"]
+CPP_SOURCES = ["bvh_build.cpp", "flatten.cpp", "scene_prep.cpp", "autotune.cpp", "scene_cache.cpp", "ingest.cpp"]
 HEADERS = ["layout.h", "host.h", "device.cuh", "estimator.cuh", "wavefront.h"]
 
 

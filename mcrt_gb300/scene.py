@@ -155,6 +155,36 @@ def vertex_alpha(vertices, normals) -> np.ndarray:
     return out
 
 
+def load_obj(path: str, transform=None):
+    """mcrt_mesh_load_obj: the triangles Scene::loadModel(path, transform, mat) adds
+    (scene.cpp:368-408) -- vertices (n, 9), vertex normals (n, 9) and consistent-normal
+    alphas (n, 3) of Mesh::genNormals.  transform: a 4x4 matrix acting on column vectors
+    (as glm::mat4 in the reference), or None."""
+    lib = N.load()
+    t = None if transform is None else np.ascontiguousarray(np.asarray(transform, np.float32).T).ravel()
+    tp = None if t is None else t.ctypes.data
+    n = ctypes.c_int64(0)
+    N.check(lib.mcrt_mesh_load_obj(path.encode(), tp, ctypes.byref(n), None, None, None), "mcrt_mesh_load_obj")
+    v = np.zeros((n.value, 9), np.float32)
+    nrm = np.zeros((n.value, 9), np.float32)
+    alpha = np.zeros((n.value, 3), np.float32)
+    N.check(lib.mcrt_mesh_load_obj(path.encode(), tp, ctypes.byref(n), v.ctypes.data, nrm.ctypes.data,
+                                   alpha.ctypes.data), "mcrt_mesh_load_obj")
+    return v, nrm, alpha
+
+
+def load_envmap_bin(path: str) -> np.ndarray:
+    """mcrt_envmap_load_bin: the (height, width, 3) float32 map EnvmapLoader reads from a
+    .bin file (envmap.cpp:98-119), top row first -- SceneDesc's envmap layout."""
+    lib = N.load()
+    w, h = ctypes.c_int32(0), ctypes.c_int32(0)
+    N.check(lib.mcrt_envmap_load_bin(path.encode(), ctypes.byref(w), ctypes.byref(h), None), "mcrt_envmap_load_bin")
+    img = np.zeros((h.value, w.value, 3), np.float32)
+    N.check(lib.mcrt_envmap_load_bin(path.encode(), ctypes.byref(w), ctypes.byref(h), img.ctypes.data),
+            "mcrt_envmap_load_bin")
+    return img
+
+
 def build_bvh(vertices, leaf_size: int = 0) -> dict:
     """mcrt_build_bvh: the library's binned-SAH tree of (n, 9) triangle vertices, in the
     form of a reference SplitBVH dump (node_box, node_info, ref_prim, ref_box; root 0)."""

@@ -142,6 +142,8 @@ def load_reference():
         lib.ref_pt_render.restype = I
         lib.ref_pt_render.argtypes = [P, I, I, I, I, I, I, P, P, P, P]
         lib.ref_pt_scene_destroy.argtypes = [P]
+        lib.ref_load_obj.restype = I
+        lib.ref_load_obj.argtypes = [ctypes.c_char_p, P, P, P, P]
         lib.ref_cornell_export.restype = I
         lib.ref_cornell_export.argtypes = [P, P, P, P]
         lib.ref_cornell_paths.restype = I

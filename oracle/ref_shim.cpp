@@ -599,3 +599,42 @@ extern "C" void ref_mesh_alpha(const float* verts, int nv, const int* faces, int
         alpha_out[i] = m.m_vertex_alpha[i];
     }
 }
+
+// Scene::loadModel (scene.cpp:368-408) on an OBJ file: the triangles it adds (vertices and
+// vertex normals), and per corner the alpha Mesh::genNormals computes for the transformed
+// mesh (loadModel itself does not copy the alphas into the triangles).  transform: 16
+// floats, column-major (glm::mat4).  Call with verts == NULL for the triangle count.
+extern "C" int ref_load_obj(const char* path, const float* transform, float* verts, float* normals, float* alpha)
+{
+    glm::mat4 T(1.0f);
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) T[c][r] = transform[4 * c + r];
+    Scene scene;
+    scene.loadModel(path, T, Material(vec3(0.5f, 0.5f, 0.5f), 0.0f, DIFF));
+    const int n = static_cast<int>(scene.numTrangles());
+    if (!verts) return n;
+    for (int i = 0; i < n; ++i)
+    {
+        const TriangleObject& t = scene.triangle(i);
+        put3(verts + 9 * i, t.a);
+        put3(verts + 9 * i + 3, t.b);
+        put3(verts + 9 * i + 6, t.c);
+        put3(normals + 9 * i, t.na);
+        put3(normals + 9 * i + 3, t.nb);
+        put3(normals + 9 * i + 6, t.nc);
+    }
+    Mesh m(path);
+    for (auto& v : m.m_verts)
+    {
+        glm::vec4 p = T * glm::vec4(v.x, v.y, v.z, 1.0f);
+        v = vec3(p.x, p.y, p.z);
+    }
+    m.genNormals();
+    for (int i = 0; i < n && i < static_cast<int>(m.m_faces.size()); ++i)
+    {
+        alpha[3 * i + 0] = m.m_vertex_alpha[m.m_faces[i].x];
+        alpha[3 * i + 1] = m.m_vertex_alpha[m.m_faces[i].y];
+        alpha[3 * i + 2] = m.m_vertex_alpha[m.m_faces[i].z];
+    }
+    return n;
+}

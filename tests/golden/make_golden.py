@@ -18,6 +18,11 @@ Fixtures (all seeded):
                            on its own Cornell box: per-pixel means of independent batches
   ref_paths_cornell.npz    the same path tracer single-threaded from the start of its global
                            random stream: every sample's radiance, for a draw-by-draw replay
+  ref_obj.npz              an OBJ file (a displaced level-2 icosphere written here, with
+                           comments and other records the reader skips), a transform, and
+                           what the reference's Scene::loadModel makes of it: triangles,
+                           vertex normals and Mesh::genNormals' alphas per corner
+                               python tests/golden/make_golden.py --only-obj
   ref_traverse_cfg1.npz    hit parity at full scale: the displaced level-8 icosphere + ground
                            (1,310,722 T, scenes.cfg1_scene(); only its SHA-256 is stored, the
                            triangles are regenerated where the test runs), 65,536 rays in each
@@ -158,6 +163,36 @@ def traverse_fixture(ref, name, desc_verts, normals, cam, rng, n_random=8192, ra
         print(f"{name}/{k}: {r.shape[0]} rays, hit {np.mean(p >= 0):.3f}")
     ref.ref_bvh_destroy(h)
     np.savez_compressed(os.path.join(OUT, f"ref_traverse_{name}.npz"), **out)
+
+
+def obj_fixture(ref):
+    rng = np.random.default_rng(7)
+    v, f = scenes.icosphere(2)
+    v = v * (1.0 + 0.2 * rng.uniform(-1, 1, (v.shape[0], 1)))
+    lines = ["# displaced level-2 icosphere", "o sphere"]
+    lines += [f"v {x:.7g} {y:.7g} {z:.7g}" for x, y, z in v]
+    lines += ["vn 0 1 0", "vt 0.5 0.5", "s off"]
+    lines += [f"f {a + 1} {b + 1} {c + 1}" for a, b, c in f]
+    # no newline after the last record: Mesh::Mesh reads tokens while !eof(), and a final
+    # newline makes it read one more face from the exhausted stream (indices 0 - 1, a face
+    # outside the vertex array); without it the reference reads exactly the file's faces
+    text = "\n".join(lines).encode()
+    # translate, rotate about y, scale (a column-major glm::mat4, as Scene::loadModel gets it)
+    c, s_ = np.cos(0.3), np.sin(0.3)
+    m = np.array([[2 * c, 0, 2 * s_, 0.25], [0, 2, 0, -0.5], [-2 * s_, 0, 2 * c, 1.0], [0, 0, 0, 1]], np.float32)
+    t16 = np.ascontiguousarray(m.T).ravel()
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "mesh.obj")
+        with open(path, "wb") as fh:
+            fh.write(text)
+        n = ref.ref_load_obj(path.encode(), ptr(t16), None, None, None)
+        verts = np.zeros((n, 9), np.float32)
+        nrm = np.zeros((n, 9), np.float32)
+        alpha = np.zeros((n, 3), np.float32)
+        ref.ref_load_obj(path.encode(), ptr(t16), ptr(verts), ptr(nrm), ptr(alpha))
+    np.savez_compressed(os.path.join(OUT, "ref_obj.npz"), obj=np.frombuffer(text, np.uint8), transform=m,
+                        verts=verts, normals=nrm, alpha=alpha)
+    print(f"obj: {n} triangles")
 
 
 def geometry_sha256(verts) -> str:
@@ -426,6 +461,9 @@ def main():
     if "--only-consistent" in sys.argv:
         consistent_fixture(ref)
         return
+    if "--only-obj" in sys.argv:
+        obj_fixture(ref)
+        return
     if "--only-cfg1" in sys.argv:
         cfg1_traverse_fixture(ref)
         return
@@ -460,6 +498,7 @@ def main():
     traverse_fixture(ref, "debugmesh", rnd, None, None, rng, n_random=16384)
     functions_fixture(ref, rng)
     cornell_image_fixture(ref)
+    obj_fixture(ref)
 
 
 if __name__ == "__main__":

@@ -153,3 +153,58 @@ def test_vertex_alpha_matches_reference_mesh(native):
     nrm = vn[f].reshape(-1, 9)
     got = vertex_alpha(soup, nrm)
     np.testing.assert_array_equal(got, va[f])
+
+
+def test_obj_loader_matches_reference_load_model(native, tmp_path):
+    """mcrt_mesh_load_obj against the reference's Scene::loadModel on the same OBJ file and
+    transform (tests/golden/ref_obj.npz): the same triangles, vertex normals and
+    Mesh::genNormals alphas, bit for bit.  The file is read again with a trailing newline,
+    CRLF line ends and "v/t/n" face indices, which must give the same triangles."""
+    from conftest import golden
+    from mcrt_gb300.scene import load_obj
+    g = golden("ref_obj.npz")
+    text = g["obj"].tobytes()
+    p = tmp_path / "mesh.obj"
+    p.write_bytes(text)
+    v, n, a = load_obj(str(p), g["transform"])
+    np.testing.assert_array_equal(v, g["verts"])
+    np.testing.assert_array_equal(n, g["normals"])
+    np.testing.assert_array_equal(a, g["alpha"])
+    lines = text.decode().split("\n")
+    variant = "\r\n".join(re.sub(r"(\d+)", r"\1/\1/1", ln) if ln.startswith("f ") else ln for ln in lines) + "\r\n"
+    q = tmp_path / "mesh_variant.obj"
+    q.write_text(variant)
+    v2, n2, a2 = load_obj(str(q), g["transform"])
+    np.testing.assert_array_equal(v2, v)
+    np.testing.assert_array_equal(n2, n)
+    np.testing.assert_array_equal(a2, a)
+
+
+def test_obj_loader_rejects_bad_files(native, tmp_path):
+    import pytest
+    from mcrt_gb300 import McrtError
+    from mcrt_gb300.scene import load_obj
+    with pytest.raises(McrtError, match="cannot open"):
+        load_obj(str(tmp_path / "missing.obj"))
+    bad = tmp_path / "bad.obj"
+    bad.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 4\n")
+    with pytest.raises(McrtError, match="beyond"):
+        load_obj(str(bad))
+    bad.write_text("v 0 0 0\nv 1 0\n")
+    with pytest.raises(McrtError, match="malformed vertex"):
+        load_obj(str(bad))
+
+
+def test_envmap_bin_round_trip_and_errors(native, tmp_path):
+    """mcrt_envmap_load_bin reads EnvmapLoader's .bin layout ({int32 w, h} + RGB floats, top
+    row first) exactly as scenes.write_envmap_bin writes it; truncated files are errors."""
+    import pytest
+    from mcrt_gb300 import McrtError, scenes
+    from mcrt_gb300.scene import load_envmap_bin
+    env = scenes.sky_envmap(64, 32, sun_diameter_deg=6.0, sun_radiance=50.0)
+    p = tmp_path / "env.bin"
+    scenes.write_envmap_bin(str(p), env)
+    np.testing.assert_array_equal(load_envmap_bin(str(p)), env.astype(np.float32))
+    p.write_bytes(p.read_bytes()[:-4])
+    with pytest.raises(McrtError, match="truncated"):
+        load_envmap_bin(str(p))

@@ -155,8 +155,8 @@ def _chain_tree(n):
     for k in range(leaves):
         node_box[inner + k] = np.concatenate([lo[k], hi[k]])
         node_info[inner + k] = (1, -1, -1, 0, k, 1)
-    tree = dict(node_box=node_box.ravel(), node_info=node_info.ravel(), ref_prim=np.arange(n, dtype=np.int32),
-                ref_box=np.concatenate([lo, hi], axis=1).ravel())
+    tree = dict(node_box=node_box, node_info=node_info, ref_prim=np.arange(n, dtype=np.int32),
+                ref_box=np.concatenate([lo, hi], axis=1))
     return v, tree
 
 
