@@ -52,6 +52,22 @@ def build_reference() -> str | None:
     return REF_SO
 
 
+SEAM_SO = os.path.join(HERE, "_ref", "libmcrt_ref_gb300.so")
+
+
+def build_seam() -> str | None:
+    """The reference build with the library behind its seams (SceneBVH backend and the
+    integrator-seam converter linked against libmcrt_gb300.so): oracle/_ref/libmcrt_ref_gb300.so.
+    Needs the reference sources and the built library; None where either is missing."""
+    from oracle.stage_reference import source_dir
+    src = source_dir()
+    lib = os.path.join(os.path.dirname(HERE), "mcrt_gb300", "_lib", "libmcrt_gb300.so")
+    if src is None or not os.path.exists(lib):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, f"REF={src}", f"-j{os.cpu_count() or 4}", "seam"], check=True)
+    return SEAM_SO
+
+
 _orc = None
 _ref = None
 
