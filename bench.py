@@ -113,8 +113,9 @@ class ClockSampler:
 # k_extend on the large configuration, from a capture of three full-queue launches of a
 # reduced case (2,097,152-ray queue, same scene and frame: 337.9 MB per launch); the bench
 # scales it by the extension rays of an average launch of the measured configuration.  An
-# upper bound for larger launches, whose rays share more of the tree lines fetched.
-K_EXTEND_DRAM_BYTES_PER_RAY = 161.1
+# upper bound for larger launches, whose rays share more of the tree lines fetched.  Keyed
+# by the node size of the traversal (64: two-child nodes).
+K_EXTEND_DRAM_BYTES_PER_RAY = {64: 161.1}
 
 
 # rows of the cfg0 / cfg1 frames the CPU port renders for cpu_baseline and --impl reference
@@ -525,13 +526,14 @@ def main():
     staged_frame_ms = sum(stage_ms)
 
     # algorithmic bytes of the two traversal kernels: a counting render of the same seeds.
-    # k_extend per extension ray: 64 B per node, 48 B per triangle tested, 32 B ray + 16 B hit;
-    # k_connect per next-event ray: nodes/triangles as above, 64 B ray + payload + meta in,
-    # 16 B result out.  Both kernels launch once per depth per wave (waves) or once per
-    # iteration (streaming).
+    # k_extend per extension ray: one node fetch per node visited (96 B for the eight-child
+    # nodes of the FAST traversal, the sectors a visit touches), 48 B per triangle tested,
+    # 32 B ray + 16 B hit; k_connect per next-event ray: nodes/triangles as above, 64 B ray +
+    # payload + meta in, 16 B result out.  Both kernels launch once per iteration.
     _, sc_cnt = sc.render(cam, seed=0, out=out, profile=PROFILE_COUNT, **kw)
-    ext_bytes = 64 * sc_cnt["ext_nodes"] + 48 * sc_cnt["ext_tris"] + (32 + 16) * sc_cnt["extension_rays"]
-    nee_bytes = 64 * sc_cnt["nee_nodes"] + 48 * sc_cnt["nee_tris"] + (64 + 16) * sc_cnt["shadow_rays"]
+    nb = sc_cnt["node_bytes"]
+    ext_bytes = nb * sc_cnt["ext_nodes"] + 48 * sc_cnt["ext_tris"] + (32 + 16) * sc_cnt["extension_rays"]
+    nee_bytes = nb * sc_cnt["nee_nodes"] + 48 * sc_cnt["nee_tris"] + (64 + 16) * sc_cnt["shadow_rays"]
     launches_per_render = max(extend_launches, 1)
     kernels = {
         "k_extend (closest-hit traversal of extension rays)": (ext_bytes, stage_ms[1], sc_cnt["extension_rays"],
@@ -548,8 +550,8 @@ def main():
     l2_peak = l2_read_peak()
     other = [k for k in kernels if k != dom][0]
     traffic = None
-    if dom.startswith("k_extend") and args.workload == "cfg1" and K_EXTEND_DRAM_BYTES_PER_RAY:
-        traffic = K_EXTEND_DRAM_BYTES_PER_RAY * kern_rays / launches_per_render
+    if dom.startswith("k_extend") and args.workload == "cfg1" and nb in K_EXTEND_DRAM_BYTES_PER_RAY:
+        traffic = K_EXTEND_DRAM_BYTES_PER_RAY[nb] * kern_rays / launches_per_render
     ob, oms = kernels[other][0], kernels[other][1]
     other_achieved = (ob / launches_per_render) / (oms / launches_per_render / 1e3) / 1e9 if oms > 0 else 0.0
 
@@ -616,6 +618,7 @@ def main():
                          "hbm": {"peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                                  "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
                          "bytes_per_ray": round(bytes_per_render / max(kern_rays, 1), 1),
+                         "node_bytes": nb,
                          "nodes_per_ray": round(kern_nodes / max(kern_rays, 1), 2),
                          "tris_per_ray": round(kern_tris / max(kern_rays, 1), 2),
                          "share_of_step": round(kern_ms / max(staged_frame_ms, 1e-9), 3),

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MCRT_ABI_VERSION 3
+#define MCRT_ABI_VERSION 4
 
 /* status codes */
 #define MCRT_OK 0
@@ -196,6 +196,9 @@ typedef struct mcrt_render_stats {
     int64_t nee_tris;
     int64_t h2d_bytes;   /* host -> device bytes copied by the call (tables, host inputs) */
     int64_t d2h_bytes;   /* device -> host bytes copied by the call (host outputs, status) */
+    int32_t node_bytes;  /* bytes of one node fetch of the traversal counted in ext_nodes / nee_nodes
+                            (96: the FAST traversal's eight-child nodes; 64: two-child nodes) */
+    int32_t reserved0;
 } mcrt_render_stats;
 
 int         mcrt_get_abi_version(void);

@@ -85,7 +85,8 @@ class RenderStats(ctypes.Structure):
     _fields_ = [("paths", c_int64), ("extension_rays", c_int64), ("shadow_rays", c_int64), ("waves", c_int32),
                 ("kernel_launches", c_int32), ("device_ms", c_float), ("stage_ms", c_float * 4),
                 ("extend_launches", c_int32), ("ext_nodes", c_int64), ("ext_tris", c_int64), ("nee_nodes", c_int64),
-                ("nee_tris", c_int64), ("h2d_bytes", c_int64), ("d2h_bytes", c_int64)]
+                ("nee_tris", c_int64), ("h2d_bytes", c_int64), ("d2h_bytes", c_int64), ("node_bytes", c_int32),
+                ("reserved0", c_int32)]
 
 
 TUNE_MAX = 16

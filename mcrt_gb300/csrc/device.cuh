@@ -5,12 +5,19 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "layout.h"
 
 // MCRT_NODE_V8: fetch a 64-B BVH node with two 256-bit loads (1) or four 128-bit loads (0).
 #ifndef MCRT_NODE_V8
 #define MCRT_NODE_V8 1
+#endif
+
+// MCRT_FAST_WIDE: the FAST traversal walks the eight-child compressed tree (1) or the
+// two-child tree (0).
+#ifndef MCRT_FAST_WIDE
+#define MCRT_FAST_WIDE 1
 #endif
 
 // MCRT_COLD: functions of materials the benchmark scenes do not use (Phong, consistent
@@ -34,15 +41,117 @@ constexpr int   kSentinel = 0x7fffffff;
 constexpr int kErrStack = 1;
 constexpr int kErrQueue = 2;
 
+// Functions marked MCRT_HDI also compile for the host, where test harnesses run the same
+// traversal code; these are the host forms of the device intrinsics they use.
+#define MCRT_HDI __host__ __device__ __forceinline__
+MCRT_HDI int ffs32(unsigned x)
+{
+#ifdef __CUDA_ARCH__
+    return __ffs(static_cast<int>(x));
+#else
+    return __builtin_ffs(static_cast<int>(x));
+#endif
+}
+MCRT_HDI int popc32(unsigned x)
+{
+#ifdef __CUDA_ARCH__
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
+}
+MCRT_HDI float bits_float(unsigned u)
+{
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+MCRT_HDI int float_bits(float f)
+{
+#ifdef __CUDA_ARCH__
+    return __float_as_int(f);
+#else
+    int i;
+    memcpy(&i, &f, 4);
+    return i;
+#endif
+}
+// byte permute with selector nibbles 0..7 (no sign replication)
+MCRT_HDI unsigned byte_perm(unsigned a, unsigned b, unsigned sel)
+{
+#ifdef __CUDA_ARCH__
+    return __byte_perm(a, b, sel);
+#else
+    const unsigned long long v = static_cast<unsigned long long>(b) << 32 | a;
+    unsigned                 r = 0;
+    for (int i = 0; i < 4; ++i) r |= static_cast<unsigned>((v >> (8 * ((sel >> (4 * i)) & 7u))) & 0xffu) << (8 * i);
+    return r;
+#endif
+}
+// round-to-nearest arithmetic without contraction (host code is compiled with
+// -ffp-contract=off, so a plain operation is one rounding there)
+MCRT_HDI float rn_add(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+MCRT_HDI float rn_sub(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+MCRT_HDI float rn_mul(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+MCRT_HDI float rn_div(float a, float b)
+{
+#ifdef __CUDA_ARCH__
+    return __fdiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+MCRT_HDI float4 ldg4(const float4* p)
+{
+#ifdef __CUDA_ARCH__
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+MCRT_HDI void or_error(int* err, int bits)
+{
+#ifdef __CUDA_ARCH__
+    atomicOr(err, bits);
+#else
+    *err |= bits;
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // float3 helpers
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float3 mk(float x, float y, float z) { return make_float3(x, y, z); }
-__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ float3 operator*(float3 a, float3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
-__device__ __forceinline__ float3 operator*(float3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float3 operator-(float3 a) { return mk(-a.x, -a.y, -a.z); }
+MCRT_HDI float3 mk(float x, float y, float z) { return make_float3(x, y, z); }
+MCRT_HDI float3 operator+(float3 a, float3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+MCRT_HDI float3 operator-(float3 a, float3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+MCRT_HDI float3 operator*(float3 a, float3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+MCRT_HDI float3 operator*(float3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+MCRT_HDI float3 operator-(float3 a) { return mk(-a.x, -a.y, -a.z); }
 __device__ __forceinline__ float  dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float3 cross3(float3 a, float3 b)
 {
@@ -55,8 +164,8 @@ __device__ __forceinline__ float3 normalize3(float3 v)
 }
 __device__ __forceinline__ float  maxc(float3 v) { return fmaxf(fmaxf(v.x, v.y), v.z); }
 __device__ __forceinline__ bool   isnan3(float3 v) { return v.x != v.x || v.y != v.y || v.z != v.z; }
-__device__ __forceinline__ float3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
-__device__ __forceinline__ float  comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+MCRT_HDI float3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
+MCRT_HDI float  comp(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 __device__ __forceinline__ float  fmax_ref(float a, float b) { return a > b ? a : b; }  // numeric.cpp f_max
 
 // ---------------------------------------------------------------------------
@@ -121,7 +230,7 @@ struct WatertightRay
     float  det_eps;
 };
 
-__device__ __forceinline__ WatertightRay make_wray(float3 o, float3 d)
+MCRT_HDI WatertightRay make_wray(float3 o, float3 d)
 {
     WatertightRay r;
     r.o = o;
@@ -146,7 +255,7 @@ __device__ __forceinline__ WatertightRay make_wray(float3 o, float3 d)
     return r;
 }
 
-__device__ __forceinline__ bool watertight(const WatertightRay& r, float3 v0, float3 v1, float3 v2, float tmin,
+MCRT_HDI bool watertight(const WatertightRay& r, float3 v0, float3 v1, float3 v2, float tmin,
                                            float tmax, float& t, float& u, float& v)
 {
     float3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
@@ -339,6 +448,169 @@ __device__ __forceinline__ bool trace_fast(const SceneView& s, float3 o, float3 
 }
 
 // ---------------------------------------------------------------------------
+// traversal: eight-child compressed nodes (WideNode, layout.h)
+// ---------------------------------------------------------------------------
+// One 96-B node: two 32-B loads, a 16-B load and the leaf mask (nodes are 32-B aligned:
+// cudaMalloc'd arrays of __align__(32) 96-B nodes; the last 12 B are padding).
+MCRT_HDI void ldg_wide(const WideNode* p, unsigned (&w)[21])
+{
+#ifndef __CUDA_ARCH__
+    memcpy(w, p, sizeof(unsigned) * 21);
+#else
+    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+        : "l"(p));
+    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8 + 32];"
+        : "=r"(w[8]), "=r"(w[9]), "=r"(w[10]), "=r"(w[11]), "=r"(w[12]), "=r"(w[13]), "=r"(w[14]), "=r"(w[15])
+        : "l"(p));
+    asm("ld.global.nc.v4.b32 {%0, %1, %2, %3}, [%4 + 64];"
+        : "=r"(w[16]), "=r"(w[17]), "=r"(w[18]), "=r"(w[19])
+        : "l"(p));
+    asm("ld.global.nc.b32 %0, [%1 + 80];" : "=r"(w[20]) : "l"(p));
+#endif
+}
+
+// 8-bit plane q of byte k of `word` as the float 2^23 + q (exact): one byte permute
+MCRT_HDI float qplane(unsigned word, int k)
+{
+    return bits_float(byte_perm(word, 0x4B000000u, 0x7650u | static_cast<unsigned>(k)));
+}
+
+// the slot-indexed bits of m moved to positions slot ^ x (x in 0..7)
+MCRT_HDI unsigned xor_permute8(unsigned m, unsigned x)
+{
+    if (x & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (x & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (x & 4u) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+    return m;
+}
+
+// Closest / any hit over the eight-child tree.  Each step visits one node: its eight child
+// boxes are tested against [tmin, best] in the node's quantised frame (per axis
+// t = (2^23 + q) a + b', a = cell / d, b' = (origin - o) / d - 2^23 a, the near plane the
+// low one for a positive direction), the triangles of the hit leaf children are tested at
+// once, and the hit inner children form a group (child block, pending bits in visiting
+// order) from which the next node is taken; a group with children left goes to the
+// per-thread stack (two ints per entry, `stack` with entries `stride` ints apart).
+// Visiting order: slot ^ octant of the direction (near to far) for closest hits; the
+// reverse for any-hit queries, whose occluders lie away from the surface the ray leaves.
+template <bool ANY, int STACK, bool COUNT>
+MCRT_HDI bool trace_wide(const SceneView& s, float3 o, float3 d, float tmin, float tmax, int* stack,
+                                           int stride, Hit& hit, int* err, TraceCount* cnt)
+{
+    const float big = 1e20f;  // 1 / d for |d| below 1e-20 (keeps 2^23 a finite)
+    const float3 inv = mk(fabsf(d.x) > 1e-20f ? 1.0f / d.x : copysignf(big, d.x),
+                          fabsf(d.y) > 1e-20f ? 1.0f / d.y : copysignf(big, d.y),
+                          fabsf(d.z) > 1e-20f ? 1.0f / d.z : copysignf(big, d.z));
+    const unsigned      oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+    const unsigned      oxor = ANY ? (oct ^ 7u) : oct;
+    const WatertightRay wr = make_wray(o, d);
+    float               best = tmax;
+    hit.prim = -1;
+    int      sp = 0;
+    int      node = 0;
+    unsigned nbase = 0, nbits = 0;
+    while (true)
+    {
+        if (COUNT) cnt->nodes++;
+        unsigned w[21];
+        ldg_wide(s.wide_nodes + node, w);
+        // per axis: cell / d and the offset, with the near / far plane words by direction sign
+        const float ax = bits_float((w[3] & 0xffu) << 23) * inv.x;
+        const float ay = bits_float(((w[3] >> 8) & 0xffu) << 23) * inv.y;
+        const float az = bits_float(((w[3] >> 16) & 0xffu) << 23) * inv.z;
+        const float bx = (bits_float(w[0]) - o.x) * inv.x - 8388608.0f * ax;
+        const float by = (bits_float(w[1]) - o.y) * inv.y - 8388608.0f * ay;
+        const float bz = (bits_float(w[2]) - o.z) * inv.z - 8388608.0f * az;
+        // w[8..9] lo.x, w[10..11] lo.y, w[12..13] lo.z, w[14..15] hi.x, w[16..17] hi.y, w[18..19] hi.z
+        const bool     px = d.x >= 0.f, py = d.y >= 0.f, pz = d.z >= 0.f;
+        const unsigned nx0 = px ? w[8] : w[14], nx1 = px ? w[9] : w[15];
+        const unsigned fx0 = px ? w[14] : w[8], fx1 = px ? w[15] : w[9];
+        const unsigned ny0 = py ? w[10] : w[16], ny1 = py ? w[11] : w[17];
+        const unsigned fy0 = py ? w[16] : w[10], fy1 = py ? w[17] : w[11];
+        const unsigned nz0 = pz ? w[12] : w[18], nz1 = pz ? w[13] : w[19];
+        const unsigned fz0 = pz ? w[18] : w[12], fz1 = pz ? w[19] : w[13];
+        unsigned hits = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+        {
+            const int      b = k & 3;
+            const unsigned wnx = k < 4 ? nx0 : nx1, wfx = k < 4 ? fx0 : fx1;
+            const unsigned wny = k < 4 ? ny0 : ny1, wfy = k < 4 ? fy0 : fy1;
+            const unsigned wnz = k < 4 ? nz0 : nz1, wfz = k < 4 ? fz0 : fz1;
+            const float tnx = fmaf(qplane(wnx, b), ax, bx), tfx = fmaf(qplane(wfx, b), ax, bx);
+            const float tny = fmaf(qplane(wny, b), ay, by), tfy = fmaf(qplane(wfy, b), ay, by);
+            const float tnz = fmaf(qplane(wnz, b), az, bz), tfz = fmaf(qplane(wfz, b), az, bz);
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, best));
+            if (tn <= tf * 1.0000004f + 1e-30f) hits |= 1u << k;
+        }
+        const unsigned imask = w[3] >> 24;
+        // triangles of the hit leaf children: tri_base + first .. + count - 1
+        unsigned lhit = hits & w[20];
+        unsigned tbits = 0;
+        while (lhit)
+        {
+            const int      sl = ffs32(lhit) - 1;
+            lhit &= lhit - 1;
+            const unsigned m = ((sl < 4 ? w[6] : w[7]) >> (8 * (sl & 3))) & 0xffu;
+            const unsigned c = ((m >> 5) & 3u) + 1u;
+            tbits |= ((1u << c) - 1u) << (m & 31u);
+        }
+        const unsigned tbase = w[5];
+        const unsigned ihit = hits & imask;
+        if (ihit)
+        {
+            nbase = w[4];
+            nbits = (xor_permute8(ihit, oxor) << 24) | imask;
+        }
+        else
+        {
+            nbits = 0;
+        }
+        while (tbits)
+        {
+            const int k = ffs32(tbits) - 1;
+            tbits &= tbits - 1;
+            if (COUNT) cnt->tris++;
+            const float4* tp = s.wide_tris + 3 * (tbase + k);
+            const float4  ta = ldg4(tp + 0), tb = ldg4(tp + 1), tc = ldg4(tp + 2);
+            float         t, u, v;
+            if (watertight(wr, xyz(ta), xyz(tb), xyz(tc), tmin, best, t, u, v))
+            {
+                best = t;
+                hit.t = t;  // u, v: recomputed for the final hit only (refine_hit)
+                hit.prim = float_bits(ta.w);
+                if (ANY) return true;
+            }
+        }
+        if ((nbits >> 24) == 0)
+        {
+            if (sp == 0) break;
+            --sp;
+            nbase = static_cast<unsigned>(stack[(2 * sp) * stride]);
+            nbits = static_cast<unsigned>(stack[(2 * sp + 1) * stride]);
+        }
+        const unsigned key = ffs32(nbits >> 24) - 1;
+        nbits &= ~(1u << (24 + key));
+        const unsigned slot = key ^ oxor;
+        node = static_cast<int>(nbase + popc32(nbits & ((1u << slot) - 1u) & 0xffu));
+        if (nbits >> 24)
+        {
+            if (2 * sp + 2 > STACK)
+            {
+                or_error(err, kErrStack);
+                return hit.prim >= 0;
+            }
+            stack[(2 * sp) * stride] = static_cast<int>(nbase);
+            stack[(2 * sp + 1) * stride] = static_cast<int>(nbits);
+            ++sp;
+        }
+    }
+    return hit.prim >= 0;
+}
+
+// ---------------------------------------------------------------------------
 // traversal: reference order and arithmetic (MCRT_TRAVERSE_REF)
 // ---------------------------------------------------------------------------
 struct RefRay
@@ -386,22 +658,22 @@ __device__ __forceinline__ bool ref_overlap(const RefRay& r, float3 lo, float3 h
     return true;
 }
 
-__device__ __forceinline__ float3 sub_rn(float3 a, float3 b)
+MCRT_HDI float3 sub_rn(float3 a, float3 b)
 {
-    return mk(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+    return mk(rn_sub(a.x, b.x), rn_sub(a.y, b.y), rn_sub(a.z, b.z));
 }
-__device__ __forceinline__ float3 cross_rn(float3 a, float3 b)
+MCRT_HDI float3 cross_rn(float3 a, float3 b)
 {
-    return mk(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
-              __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+    return mk(rn_sub(rn_mul(a.y, b.z), rn_mul(a.z, b.y)), rn_sub(rn_mul(a.z, b.x), rn_mul(a.x, b.z)),
+              rn_sub(rn_mul(a.x, b.y), rn_mul(a.y, b.x)));
 }
-__device__ __forceinline__ float dot_rn(float3 a, float3 b)
+MCRT_HDI float dot_rn(float3 a, float3 b)
 {
-    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+    return rn_add(rn_add(rn_mul(a.x, b.x), rn_mul(a.y, b.y)), rn_mul(a.z, b.z));
 }
 
 // rayTriangleIntersect, MOLLER_TRUMBORE branch (triangle.cpp:13-51)
-__device__ __forceinline__ bool ref_mt(float3 orig, float3 dir, float3 v0, float3 v1, float3 v2, float& t, float& u,
+MCRT_HDI bool ref_mt(float3 orig, float3 dir, float3 v0, float3 v1, float3 v2, float& t, float& u,
                                        float& v)
 {
     float3 v0v1 = sub_rn(v1, v0);
@@ -409,14 +681,14 @@ __device__ __forceinline__ bool ref_mt(float3 orig, float3 dir, float3 v0, float
     float3 pvec = cross_rn(dir, v0v2);
     float  det = dot_rn(v0v1, pvec);
     if (fabsf(det) < kEpsDet) return false;
-    float  invDet = __fdiv_rn(1.0f, det);
+    float  invDet = rn_div(1.0f, det);
     float3 tvec = sub_rn(orig, v0);
-    u = __fmul_rn(dot_rn(tvec, pvec), invDet);
+    u = rn_mul(dot_rn(tvec, pvec), invDet);
     if (u < 0.f || u > 1.f) return false;
     float3 qvec = cross_rn(tvec, v0v1);
-    v = __fmul_rn(dot_rn(dir, qvec), invDet);
-    if (v < 0.f || __fadd_rn(u, v) > 1.f) return false;
-    t = __fmul_rn(dot_rn(v0v2, qvec), invDet);
+    v = rn_mul(dot_rn(dir, qvec), invDet);
+    if (v < 0.f || rn_add(u, v) > 1.f) return false;
+    t = rn_mul(dot_rn(v0v2, qvec), invDet);
     return true;
 }
 
@@ -486,10 +758,10 @@ __device__ __forceinline__ bool trace_ref(const SceneView& s, float3 o, float3 d
 // The watertight test decides which triangle is closest; the reported t, u, v of that
 // one triangle are then recomputed with the reference's Moller-Trumbore arithmetic (each
 // formula lands ~3 ulp from the exact t, on either side).
-__device__ __forceinline__ void refine_hit(const SceneView& s, float3 o, float3 d, float tmin, Hit& hit)
+MCRT_HDI void refine_hit(const SceneView& s, float3 o, float3 d, float tmin, Hit& hit)
 {
     const float4* pv = s.prim_verts + 3 * hit.prim;
-    const float3  va = xyz(__ldg(pv)), vb = xyz(__ldg(pv + 1)), vc = xyz(__ldg(pv + 2));
+    const float3  va = xyz(ldg4(pv)), vb = xyz(ldg4(pv + 1)), vc = xyz(ldg4(pv + 2));
     float         t, u, v;
     if (ref_mt(o, d, va, vb, vc, t, u, v) && t > tmin)
     {
@@ -502,7 +774,7 @@ __device__ __forceinline__ void refine_hit(const SceneView& s, float3 o, float3 
     // (two registers fewer in its loop); the same inputs give the same result again
     hit.u = 0.f;
     hit.v = 0.f;
-    if (watertight(make_wray(o, d), va, vb, vc, tmin, __int_as_float(0x7f800000), t, u, v))
+    if (watertight(make_wray(o, d), va, vb, vc, tmin, bits_float(0x7f800000u), t, u, v))
     {
         hit.u = u;
         hit.v = v;
@@ -517,7 +789,11 @@ __device__ __forceinline__ bool trace_ray(const SceneView& s, int mode, float3 o
                                           int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr)
 {
     if (REFM && mode == 1) return trace_ref<ANY, STACK>(s, o, d, tmin, tmax, stack, stride, hit, err);
+#if MCRT_FAST_WIDE
+    bool found = trace_wide<ANY, STACK, COUNT>(s, o, d, tmin, tmax, stack, stride, hit, err, cnt);
+#else
     bool found = trace_fast<ANY, STACK, COUNT>(s, o, d, tmin, tmax, stack, stride, hit, err, cnt);
+#endif
     if (!ANY && found) refine_hit(s, o, d, tmin, hit);
     return found;
 }

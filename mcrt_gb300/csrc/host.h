@@ -36,11 +36,25 @@ struct FlatBVH
     std::vector<RefNode>  ref_nodes;
     std::vector<RefPrim>  ref_prims;
     int                   max_depth = 0;
+    std::vector<WideNode> wide_nodes;
+    std::vector<float4>   wide_tris;  // 3 per leaf-child reference
+    int                   wide_depth = 0;
 };
 
 // Validates the tree and emits both device layouts in depth-first order.
 // Returns an empty string on success, else an error message.
 std::string flatten_tree(const BinaryTree& tree, const float* vertices, int64_t num_tris, FlatBVH& out);
+
+// Collapses a validated binary tree into the eight-child layout (WideNode, wide_tris):
+// an SAH-optimal choice of each wide node's children among its binary descendants,
+// octant slot assignment and outward-rounded 8-bit child boxes.  c_tri: the cost of a
+// triangle test relative to a wide-node visit.
+std::string build_wide(const BinaryTree& tree, const float* vertices, int64_t num_tris, FlatBVH& out,
+                       float c_tri = 0.4f);
+// Checks every index a traversal of the eight-child layout follows (child blocks, leaf
+// triangle ranges, primitive ids) and the tree depth; an empty string when all are valid.
+std::string validate_wide(const std::vector<WideNode>& nodes, const std::vector<float4>& tris, int64_t num_prims,
+                          int* depth);
 
 struct HostScene
 {

@@ -1055,6 +1055,7 @@ struct mcrt_scene
     std::vector<void*> allocs;
     int64_t            fast_nodes = 0, ref_nodes = 0, refs = 0, bytes = 0;
     int                bvh_depth = 0;
+    int                wide_depth = 0;  // levels of the eight-child tree
     int                device = 0;
     int                num_materials = 0;
     MaterialGPU*       d_materials = nullptr;
@@ -1067,6 +1068,17 @@ struct mcrt_scene
 };
 
 namespace {
+
+// The traversal-stack depth a job needs, in the units of the "+ 2 < kStack" checks: the
+// REF traversal walks the two-child tree (one int per level), the FAST traversal the
+// eight-child tree (two ints per level).
+int stack_depth(const mcrt_scene* s, int traverse)
+{
+#if MCRT_FAST_WIDE
+    if (traverse != MCRT_TRAVERSE_REF) return 2 * s->wide_depth;
+#endif
+    return s->bvh_depth;
+}
 
 template <class T>
 int upload(mcrt_scene* s, const std::vector<T>& v, const T** out)
@@ -1737,7 +1749,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
         total += px * p.spp;
         pix_spp[j] = p.spp;
         max_depth = std::max(max_depth, p.max_depth);
-        bvh_depth = std::max(bvh_depth, scenes[j]->bvh_depth);
+        bvh_depth = std::max(bvh_depth, stack_depth(scenes[j], p.traverse));
         if (ptr_mode == MCRT_PTR_DEVICE)
         {
             dev_images[j] = outs[j];
@@ -1827,6 +1839,7 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
         stats->ext_tris = static_cast<int64_t>(hstats[3]);
         stats->nee_nodes = static_cast<int64_t>(hstats[4]);
         stats->nee_tris = static_cast<int64_t>(hstats[5]);
+        stats->node_bytes = MCRT_FAST_WIDE ? static_cast<int32_t>(sizeof(WideNode)) : static_cast<int32_t>(sizeof(FastNode));
         int64_t img_bytes = 0;
         for (int j = 0; j < num_jobs; ++j) img_bytes += 12 * static_cast<int64_t>(cams[j].width) * cams[j].height;
         stats->h2d_bytes = static_cast<int64_t>(sizeof(JobGPU)) * num_jobs + run.table_bytes;
@@ -1991,6 +2004,10 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
     up(hs.env_guide_m, &egm);
     up(hs.env_guide_c, &egc);
     up(hs.prim_alpha, &pa);
+    const WideNode* wn;
+    const float4*   wt;
+    up(hs.bvh.wide_nodes, &wn);
+    up(hs.bvh.wide_tris, &wt);
     if (rc != MCRT_OK)
     {
         std::string msg = g_err;
@@ -2001,6 +2018,8 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
     v.prim_alpha = pa;
     v.fast_nodes = fn;
     v.fast_tris = ft;
+    v.wide_nodes = wn;
+    v.wide_tris = wt;
     v.ref_nodes = rn;
     v.ref_prims = rp;
     v.prim_verts = pv;
@@ -2025,6 +2044,7 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
     s->ref_nodes = static_cast<int64_t>(hs.bvh.ref_nodes.size());
     s->refs = static_cast<int64_t>(hs.bvh.ref_prims.size());
     s->bvh_depth = hs.bvh.max_depth;
+    s->wide_depth = hs.bvh.wide_depth;
     s->desc_hash = desc_hash;
     *out = s;
     return MCRT_OK;
@@ -2033,7 +2053,7 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
 // downloads a scene's prepared arrays (the inverse of scene_from_host)
 int scene_to_host(const mcrt_scene* s, HostScene& hs, int64_t& num_tris, uint64_t& desc_hash)
 {
-    if (s->array_bytes.size() != 15) return fail(MCRT_ERR_INTERNAL, "scene arrays not recorded");
+    if (s->array_bytes.size() != 17) return fail(MCRT_ERR_INTERNAL, "scene arrays not recorded");
     CK(cudaSetDevice(s->device));
     const SceneView& v = s->view;
     int              k = 0, rc = MCRT_OK;
@@ -2061,11 +2081,14 @@ int scene_to_host(const mcrt_scene* s, HostScene& hs, int64_t& num_tris, uint64_
     down(hs.env_guide_m, v.env_guide_m);
     down(hs.env_guide_c, v.env_guide_c);
     down(hs.prim_alpha, v.prim_alpha);
+    down(hs.bvh.wide_nodes, v.wide_nodes);
+    down(hs.bvh.wide_tris, v.wide_tris);
     hs.light_area = v.light_area;
     hs.env_w = v.env_w;
     hs.env_h = v.env_h;
     hs.env_norm = v.env_norm;
     hs.bvh.max_depth = s->bvh_depth;
+    hs.bvh.wide_depth = s->wide_depth;
     num_tris = v.num_prims;
     desc_hash = s->desc_hash;
     return rc;
@@ -2080,7 +2103,7 @@ int set_error(int code, const std::string& msg) { return fail(code, msg); }
 
 const SceneView& scene_view(const mcrt_scene* s) { return s->view; }
 int              scene_device(const mcrt_scene* s) { return s->device; }
-int              scene_bvh_depth(const mcrt_scene* s) { return s->bvh_depth; }
+int              scene_stack_depth(const mcrt_scene* s, int traverse) { return stack_depth(s, traverse); }
 
 }  // namespace mcrt
 
@@ -2161,7 +2184,8 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
     if (traverse != MCRT_TRAVERSE_FAST && traverse != MCRT_TRAVERSE_REF)
         return fail(MCRT_ERR_INVALID_ARGUMENT, "unknown traversal mode");
     if (n == 0) return MCRT_OK;
-    if (s->bvh_depth + 2 >= kStack) return fail(MCRT_ERR_STACK_OVERFLOW, "BVH deeper than the traversal stack");
+    if (stack_depth(s, traverse) + 2 >= kStack)
+        return fail(MCRT_ERR_STACK_OVERFLOW, "BVH deeper than the traversal stack");
     CK(cudaSetDevice(s->device));
     cudaStream_t  st = static_cast<cudaStream_t>(stream);
     const float4* d_rays = reinterpret_cast<const float4*>(rays);
@@ -2302,7 +2326,8 @@ static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_came
         if (rc) return rc;
         if (!dLs[j]) return fail(MCRT_ERR_INVALID_ARGUMENT, "null dL/dimage buffer");
         if (params[j].ptr_mode != ptr_mode) return fail(MCRT_ERR_INVALID_ARGUMENT, "all jobs share ptr_mode");
-        if (scenes[j]->bvh_depth + 2 >= kStack) return fail(MCRT_ERR_STACK_OVERFLOW, "BVH deeper than the stack");
+        if (stack_depth(scenes[j], params[j].traverse) + 2 >= kStack)
+            return fail(MCRT_ERR_STACK_OVERFLOW, "BVH deeper than the stack");
     }
     if ((n_albedo > 0 && !d_albedo) || (n_emis > 0 && !d_emis) || n_albedo < 0 || n_emis < 0)
         return fail(MCRT_ERR_INVALID_ARGUMENT, "null gradient buffer");
@@ -2384,7 +2409,7 @@ static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_came
     for (int j = 0; j < num_jobs; ++j)
     {
         max_depth = std::max(max_depth, params[j].max_depth);
-        bvh_depth = std::max(bvh_depth, scenes[j]->bvh_depth);
+        bvh_depth = std::max(bvh_depth, stack_depth(scenes[j], params[j].traverse));
         small_ids = small_ids && scenes[j]->num_materials <= 65536;
     }
     if (params[0].schedule == MCRT_SCHEDULE_STREAM && max_depth < kAdjLog && small_ids)

@@ -37,6 +37,33 @@ struct __align__(64) FastNode
     int4   n3;  // child0, child1, count0, count1
 };
 
+// Eight-child node of the FAST traversal (96 B, three 32-B loads), after the compressed
+// wide BVH of Ylitie, Karras and Laine (HPG 2017): the children's boxes are quantised to
+// 8 bits per plane on a per-node grid (origin p, power-of-two cell size 2^(e - 127) per
+// axis, every child box rounded outwards), inner children are stored contiguously from
+// child_base in slot order, and the leaf children's triangles contiguously from tri_base.
+// Slots are assigned so that visiting them in the order slot ^ octant(ray direction)
+// approximates front-to-back order for every octant.
+//   w0: p.x, p.y, p.z, (e.x | e.y << 8 | e.z << 16 | imask << 24)
+//   w1: child_base, tri_base, meta[0..3], meta[4..7]
+//       meta[s] = leaf child: 0x80 | (count - 1) << 5 | first, its triangles tri_base + first
+//       .. + count - 1 (count 1..4, first + count <= 32); 0 otherwise (inner children are
+//       the bits of imask)
+//   w2: lo.x[0..7], lo.y[0..7]            (8-bit quantised planes, byte s = slot s)
+//   w3: lo.z[0..7], hi.x[0..7]
+//   w4: hi.y[0..7], hi.z[0..7]
+//   w5: unused
+// An empty slot has lo = 255 > hi = 0 on every axis, so no ray enters it.
+struct __align__(32) WideNode
+{
+    float4 w0;
+    int4   w1;
+    int4   w2, w3, w4;
+    int4   w5;
+};
+constexpr int kWideMaxLeafTris = 4;   // triangles per leaf child
+constexpr int kWideMaxNodeTris = 32;  // triangles per node (the hit mask of a node's leaves)
+
 // inner: a = left, b = (right << 2) | split_axis;  leaf: a = ~ref_begin, b = ref_count
 struct __align__(32) RefNode
 {
@@ -77,6 +104,8 @@ struct SceneView
 {
     const FastNode*    fast_nodes;
     const float4*      fast_tris;
+    const WideNode*    wide_nodes;  // the FAST traversal's eight-child tree
+    const float4*      wide_tris;   // its leaf triangles {v0, prim}, {v1}, {v2} in node order
     const RefNode*     ref_nodes;
     const RefPrim*     ref_prims;
     const float4*      prim_verts;

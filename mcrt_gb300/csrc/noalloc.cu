@@ -119,7 +119,7 @@ extern "C" int mcrt_render_noalloc(mcrt_scene* scene, const mcrt_camera* camera,
         if (params->ptr_mode != MCRT_PTR_DEVICE)
             return set_error(MCRT_ERR_INVALID_ARGUMENT,
                              "mcrt_render_noalloc takes device buffers only (ptr_mode = MCRT_PTR_DEVICE)");
-        if (scene_bvh_depth(scene) + 2 >= kStack)
+        if (scene_stack_depth(scene, params->traverse) + 2 >= kStack)
             return set_error(MCRT_ERR_STACK_OVERFLOW, "BVH deeper than the traversal stack");
         if (params->spp > kNoAllocPaths)
             return set_error(MCRT_ERR_INVALID_ARGUMENT,

@@ -1,11 +1,11 @@
-// Scene cache files: a prepared device scene (both node layouts, leaf triangles, shading
+// Scene cache files: a prepared device scene (all three node layouts, leaf triangles, shading
 // arrays, light and environment-map sampling tables) written to disk and uploaded again
 // without running the builder, the flattener or the table construction.
 //
 // Format (little-endian, version kFormat):
-//   "MCRTSCN\0"  u32 format  u32 array count (15)  u64 description hash  i64 triangles
-//   f32 light_area  f32 env_norm  i32 env_w  i32 env_h  i32 bvh_depth  i32 0
-//   15 x { u32 element size, u32 0, i64 bytes }  -- the arrays of scene_from_host, in order
+//   "MCRTSCN\0"  u32 format  u32 array count (17)  u64 description hash  i64 triangles
+//   f32 light_area  f32 env_norm  i32 env_w  i32 env_h  i32 bvh_depth  i32 wide_depth
+//   17 x { u32 element size, u32 0, i64 bytes }  -- the arrays of scene_from_host, in order
 //   the arrays' bytes, in order
 //   u64 checksum (FNV-1a 64 over 64-bit words) of everything before it
 // The description hash (mcrt_scene_desc_hash) covers every input of the scene and the
@@ -25,8 +25,8 @@
 namespace mcrt {
 namespace {
 
-constexpr uint32_t kFormat = 3;
-constexpr int      kArrays = 15;
+constexpr uint32_t kFormat = 4;
+constexpr int      kArrays = 17;
 const char         kMagic[8] = {'M', 'C', 'R', 'T', 'S', 'C', 'N', '\0'};
 
 // FNV-1a 64 over little-endian 64-bit words (remaining bytes one at a time): the hash of
@@ -62,7 +62,7 @@ struct Fnv
 const uint32_t kElem[kArrays] = {sizeof(FastNode), sizeof(float4), sizeof(RefNode),     sizeof(RefPrim), sizeof(float4),
                                  sizeof(float4),   sizeof(int32_t), sizeof(LightGPU),   sizeof(MaterialGPU),
                                  sizeof(float4),   sizeof(float),   sizeof(float),      sizeof(int32_t), sizeof(int32_t),
-                                 sizeof(float4)};
+                                 sizeof(float4),   sizeof(WideNode), sizeof(float4)};
 
 struct Header
 {
@@ -73,7 +73,7 @@ struct Header
     int64_t  num_tris;
     float    light_area;
     float    env_norm;
-    int32_t  env_w, env_h, bvh_depth, pad;
+    int32_t  env_w, env_h, bvh_depth, wide_depth;
     struct
     {
         uint32_t elem, pad;
@@ -99,6 +99,8 @@ void for_each_array(HostScene& hs, F&& f)
     f(hs.env_guide_m);
     f(hs.env_guide_c);
     f(hs.prim_alpha);
+    f(hs.bvh.wide_nodes);
+    f(hs.bvh.wide_tris);
 }
 
 inline int32_t ibits(float f)
@@ -147,6 +149,10 @@ std::string validate(const HostScene& hs, int64_t num_tris)
         const int32_t p = ibits(r.lo.w);
         if (p < 0 || p >= num_tris) return "reference primitive out of range";
     }
+    int wide_depth = 0;
+    std::string werr = validate_wide(hs.bvh.wide_nodes, hs.bvh.wide_tris, num_tris, &wide_depth);
+    if (!werr.empty()) return werr;
+    if (wide_depth != hs.bvh.wide_depth) return "wide BVH depth does not match the header";
     const int64_t mats = static_cast<int64_t>(hs.materials.size());
     for (size_t k = 0; k < hs.prim_shade.size(); k += 3)
     {
@@ -256,6 +262,7 @@ extern "C" int mcrt_scene_save(const mcrt_scene* scene, const char* path)
         hd.env_w = hs.env_w;
         hd.env_h = hs.env_h;
         hd.bvh_depth = hs.bvh.max_depth;
+        hd.wide_depth = hs.bvh.wide_depth;
         int k = 0;
         for_each_array(hs, [&](auto& v) {
             hd.a[k].elem = kElem[k];
@@ -335,9 +342,10 @@ extern "C" int mcrt_scene_load(const char* path, uint64_t expected_hash, mcrt_sc
         hs.env_w = hd.env_w;
         hs.env_h = hd.env_h;
         hs.bvh.max_depth = hd.bvh_depth;
+        hs.bvh.wide_depth = hd.wide_depth;
         if (hs.env_w < 0 || hs.env_h < 0 ||
             hs.env_rgb.size() != static_cast<size_t>(hs.env_w) * static_cast<size_t>(hs.env_h) ||
-            hs.bvh.fast_nodes.empty() || hs.materials.empty())
+            hs.bvh.fast_nodes.empty() || hs.bvh.wide_nodes.empty() || hs.materials.empty())
             return set_error(MCRT_ERR_IO, "mcrt_scene_load: inconsistent scene arrays");
         const std::string bad = validate(hs, hd.num_tris);
         if (!bad.empty()) return set_error(MCRT_ERR_IO, "mcrt_scene_load: " + bad);

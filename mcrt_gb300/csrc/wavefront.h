@@ -172,6 +172,6 @@ int set_error(int code, const std::string& msg);
 // read-only facts about a scene handle
 const SceneView& scene_view(const mcrt_scene* s);
 int              scene_device(const mcrt_scene* s);
-int              scene_bvh_depth(const mcrt_scene* s);
+int              scene_stack_depth(const mcrt_scene* s, int traverse);  // see the stack checks
 
 }  // namespace mcrt

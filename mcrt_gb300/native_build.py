@@ -21,7 +21,8 @@ LIB = os.path.join(LIB_DIR, "libmcrt_gb300.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["kernels.cu", "noalloc.cu", "film.cu", "probe.cu"]
-CPP_SOURCES = ["bvh_build.cpp", "flatten.cpp", "scene_prep.cpp", "autotune.cpp", "scene_cache.cpp", "ingest.cpp"]
+CPP_SOURCES = ["bvh_build.cpp", "flatten.cpp", "scene_prep.cpp", "autotune.cpp", "scene_cache.cpp", "ingest.cpp",
+               "wide_build.cpp"]
 HEADERS = ["layout.h", "host.h", "device.cuh", "estimator.cuh", "wavefront.h"]
 
 
@@ -46,6 +47,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(LIB_DIR, exist_ok=True)
+    # MCRT_NVCC_DEFINES: extra -D options for the CUDA sources (e.g. -DMCRT_FAST_WIDE=0 builds
+    # the two-child FAST traversal); a change of them rebuilds everything
+    defines = os.environ.get("MCRT_NVCC_DEFINES", "").split()
+    if any(not d.startswith("-D") for d in defines):
+        raise ValueError("MCRT_NVCC_DEFINES takes -D options only")
+    stamp = os.path.join(LIB_DIR, "defines.txt")
+    old = open(stamp).read() if os.path.exists(stamp) else ""
+    if old != " ".join(defines):
+        force = True
+        with open(stamp, "w") as f:
+            f.write(" ".join(defines))
     include = os.path.join(os.path.dirname(HERE), "include", "mcrt_gb300.h")
     headers = [os.path.join(CSRC, h) for h in HEADERS] + [include]
     jobs = []
@@ -56,7 +68,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append([nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                         "-Xptxas", "-warn-spills", "-c", s, "-o", o])
+                         "-Xptxas", "-warn-spills"] + defines + ["-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(LIB_DIR, src + ".o")

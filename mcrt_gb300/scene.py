@@ -396,7 +396,7 @@ def stats_dict(st: N.RenderStats) -> dict:
             "rays": st.extension_rays + st.shadow_rays, "waves": st.waves, "kernel_launches": st.kernel_launches,
             "device_ms": st.device_ms, "stage_ms": list(st.stage_ms), "extend_launches": st.extend_launches,
             "ext_nodes": st.ext_nodes, "ext_tris": st.ext_tris, "nee_nodes": st.nee_nodes, "nee_tris": st.nee_tris,
-            "h2d_bytes": st.h2d_bytes, "d2h_bytes": st.d2h_bytes}
+            "h2d_bytes": st.h2d_bytes, "d2h_bytes": st.d2h_bytes, "node_bytes": st.node_bytes}
 
 
 def render_batch(scenes: list, cameras: list, params: list, outs: list | None = None):

