@@ -287,62 +287,75 @@ def _timed(fn, reps=1):
 
 
 def bench_cfg2(args):
-    """64 procedural scenes of uneven size: one batched wavefront (CUDA graph per wave)
-    against the same renders issued scene by scene."""
+    """64 procedural scenes of uneven size: one batched wavefront against the same renders
+    issued scene by scene (streaming per scene, and the wave schedule per scene).
+    --cfg2-part batched|sequential|waves runs one of the three alone (launch lists);
+    --no-autotune keeps the library's default launch configuration."""
     import torch
     from mcrt_gb300 import GpuScene, autotune, render_batch, scenes
     jobs = scenes.cfg2_jobs(64)
     t0 = time.time()
     gs = [GpuScene(d) for d, _, _ in jobs]
     setup_s = time.time() - t0
-    # the same 64 scenes from scene cache files (mcrt_scene_save / mcrt_scene_load)
-    import tempfile
-    with tempfile.TemporaryDirectory() as tmp:
-        paths = [os.path.join(tmp, f"s{k}.mcrt") for k in range(len(gs))]
-        for g, pth in zip(gs, paths):
-            g.save(pth)
-        t0 = time.time()
-        loaded = [GpuScene.load(pth, d) for pth, (d, _, _) in zip(paths, jobs)]
-        load_s = time.time() - t0
-        cache_mb = sum(os.path.getsize(pth) for pth in paths) / 1e6
-        for g in loaded:
-            g.close()
+    part = args.cfg2_part
+    load_s = cache_mb = None
+    if part == "all":
+        # the same 64 scenes from scene cache files (mcrt_scene_save / mcrt_scene_load)
+        with tempfile.TemporaryDirectory() as tmp:
+            paths = [os.path.join(tmp, f"s{k}.mcrt") for k in range(len(gs))]
+            for g, pth in zip(gs, paths):
+                g.save(pth)
+            t0 = time.time()
+            loaded = [GpuScene.load(pth, d) for pth, (d, _, _) in zip(paths, jobs)]
+            load_s = time.time() - t0
+            cache_mb = sum(os.path.getsize(pth) for pth in paths) / 1e6
+            for g in loaded:
+                g.close()
     cams = [c for _, c, _ in jobs]
     params = [dict(p, use_graph=True, schedule=args.schedule_id) for _, _, p in jobs]
     outs = [torch.empty((c.height, c.width, 3), device="cuda") for c in cams]
-    t0 = time.time()
-    params, tune = autotune(gs, cams, params)  # queue capacity and kernel variant for the batch
-    tune_s = time.time() - t0
-    render_batch(gs, cams, params, outs)  # warm-up
-    for s, c, p, o in zip(gs, cams, jobs, outs):
-        s.render(c, out=o, schedule=args.schedule_id, **p[2])
-    tb, (_, stb) = _timed(lambda: render_batch(gs, cams, params, outs), reps=args.steps)
+    tune, tune_s = None, 0.0
+    if part in ("all", "batched") and not args.no_autotune:
+        t0 = time.time()
+        params, tune = autotune(gs, cams, params)  # queue capacity and kernel variant for the batch
+        tune_s = time.time() - t0
+
     def sequential():
         tot = 0
         for s, c, (_, _, p), o in zip(gs, cams, jobs, outs):
             _, st = s.render(c, out=o, schedule=args.schedule_id, **p)
             tot += st["rays"]
         return tot
-    ts, seq_rays = _timed(sequential, reps=args.steps)
 
     def sequential_waves():
         for s, c, (_, _, p), o in zip(gs, cams, jobs, outs):
             s.render(c, out=o, schedule=1, **p)
-    sequential_waves()
-    tw, _ = _timed(sequential_waves, reps=args.steps)
-    paths = stb["paths"]
+
     line = {"workload": "cfg2: 64 scenes, displaced icospheres 1k-500k T in Cornell shells, res {128..1024}^2, "
-                        "spp 1..64, depth 4..16", "paths": paths, "rays": stb["rays"],
-            "batched_ms": round(tb * 1e3, 2), "sequential_ms": round(ts * 1e3, 2),
-            "batched_mrays_s": round(stb["rays"] / tb / 1e6, 1), "sequential_mrays_s": round(seq_rays / ts / 1e6, 1),
-            "batched_msamples_s": round(paths / tb / 1e6, 1), "speedup_batched_vs_sequential": round(ts / tb, 3),
-            "sequential_waves_ms": round(tw * 1e3, 2), "speedup_batched_vs_sequential_waves": round(tw / tb, 3),
-            "autotune": {"seconds": round(tune_s, 2), "probe_paths": tune["probe_paths"],
-                         "chosen": tune["candidates"][tune["chosen"]], "candidates": len(tune["candidates"])},
-            "schedule": args.schedule, "waves": stb["waves"], "scene_setup_s": round(setup_s, 1),
-            "scene_cache_load_s": round(load_s, 2), "scene_cache_mb": round(cache_mb, 1),
-            "triangles": int(sum(d.num_triangles
-                                                                                               for d, _, _ in jobs))}
+                        "spp 1..64, depth 4..16", "part": part, "schedule": args.schedule,
+            "scene_setup_s": round(setup_s, 1),
+            "triangles": int(sum(d.num_triangles for d, _, _ in jobs))}
+    if part in ("all", "batched"):
+        render_batch(gs, cams, params, outs)  # warm-up
+        tb, (_, stb) = _timed(lambda: render_batch(gs, cams, params, outs), reps=args.steps)
+        line.update({"paths": stb["paths"], "rays": stb["rays"], "batched_ms": round(tb * 1e3, 2),
+                     "batched_mrays_s": round(stb["rays"] / tb / 1e6, 1),
+                     "batched_msamples_s": round(stb["paths"] / tb / 1e6, 1), "waves": stb["waves"]})
+        if tune is not None:
+            line["autotune"] = {"seconds": round(tune_s, 2), "probe_paths": tune["probe_paths"],
+                                "chosen": tune["candidates"][tune["chosen"]], "candidates": len(tune["candidates"])}
+    if part in ("all", "sequential"):
+        sequential()
+        ts, seq_rays = _timed(sequential, reps=args.steps)
+        line.update({"sequential_ms": round(ts * 1e3, 2), "sequential_mrays_s": round(seq_rays / ts / 1e6, 1)})
+    if part in ("all", "waves"):
+        sequential_waves()
+        tw, _ = _timed(sequential_waves, reps=args.steps)
+        line["sequential_waves_ms"] = round(tw * 1e3, 2)
+    if part == "all":
+        line.update({"speedup_batched_vs_sequential": round(line["sequential_ms"] / line["batched_ms"], 3),
+                     "speedup_batched_vs_sequential_waves": round(line["sequential_waves_ms"] / line["batched_ms"], 3),
+                     "scene_cache_load_s": round(load_s, 2), "scene_cache_mb": round(cache_mb, 1)})
     print(json.dumps(line), flush=True)
 
 
@@ -419,6 +432,9 @@ def main():
     ap.add_argument("--path-chunk", type=int, default=0, help="path slots in flight (0: library default)")
     ap.add_argument("--variant", type=int, default=0, help="traversal kernel variant bits (0: default policy)")
     ap.add_argument("--autotune", action="store_true", help="pick path_chunk / variant with mcrt_autotune first")
+    ap.add_argument("--cfg2-part", default="all", choices=["all", "batched", "sequential", "waves"],
+                    help="cfg2: run the batched render, the per-scene renders or the per-scene wave renders alone")
+    ap.add_argument("--no-autotune", action="store_true", help="cfg2: the library's default launch configuration")
     ap.add_argument("--quick", action="store_true",
                     help="only the timed renders, stage split and counts (profiling small cases)")
     ap.add_argument("--fp64-rows", type=int, nargs=2, default=None,

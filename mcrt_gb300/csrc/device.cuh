@@ -15,9 +15,12 @@
 #endif
 
 // MCRT_FAST_WIDE: the FAST traversal walks the eight-child compressed tree (1) or the
-// two-child tree (0).
+// two-child tree (0, the default).  Per cfg1 frame, extension / next-event kernels: two-child
+// 45.3 / 33.5 ms, eight-child 60.1 / 54.4 ms (10.4 instead of 24.1 node visits per ray, but
+// each visit costs about three times the instructions, and the kernels are bound by issue
+// and divergence with the tree in L2, not by the node fetches).
 #ifndef MCRT_FAST_WIDE
-#define MCRT_FAST_WIDE 1
+#define MCRT_FAST_WIDE 0
 #endif
 
 // MCRT_COLD: functions of materials the benchmark scenes do not use (Phong, consistent
@@ -476,6 +479,35 @@ MCRT_HDI float qplane(unsigned word, int k)
     return bits_float(byte_perm(word, 0x4B000000u, 0x7650u | static_cast<unsigned>(k)));
 }
 
+// three-input minimum / maximum (one instruction on sm_100 and later)
+#ifndef MCRT_WIDE_MAX3
+#define MCRT_WIDE_MAX3 0
+#endif
+MCRT_HDI float fmax3f(float a, float b, float c)
+{
+#if defined(__CUDA_ARCH__) && MCRT_WIDE_MAX3
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fmaxf(fmaxf(a, b), c);
+#endif
+}
+MCRT_HDI float fmin3f(float a, float b, float c)
+{
+#if defined(__CUDA_ARCH__) && MCRT_WIDE_MAX3
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fminf(fminf(a, b), c);
+#endif
+}
+#ifndef MCRT_WIDE_UNROLL
+#define MCRT_WIDE_UNROLL 8
+#endif
+constexpr int kWideUnroll = MCRT_WIDE_UNROLL;
+
 // the slot-indexed bits of m moved to positions slot ^ x (x in 0..7)
 MCRT_HDI unsigned xor_permute8(unsigned m, unsigned x)
 {
@@ -531,7 +563,7 @@ MCRT_HDI bool trace_wide(const SceneView& s, float3 o, float3 d, float tmin, flo
         const unsigned nz0 = pz ? w[12] : w[18], nz1 = pz ? w[13] : w[19];
         const unsigned fz0 = pz ? w[18] : w[12], fz1 = pz ? w[19] : w[13];
         unsigned hits = 0;
-#pragma unroll
+#pragma unroll kWideUnroll
         for (int k = 0; k < 8; ++k)
         {
             const int      b = k & 3;
@@ -541,8 +573,8 @@ MCRT_HDI bool trace_wide(const SceneView& s, float3 o, float3 d, float tmin, flo
             const float tnx = fmaf(qplane(wnx, b), ax, bx), tfx = fmaf(qplane(wfx, b), ax, bx);
             const float tny = fmaf(qplane(wny, b), ay, by), tfy = fmaf(qplane(wfy, b), ay, by);
             const float tnz = fmaf(qplane(wnz, b), az, bz), tfz = fmaf(qplane(wfz, b), az, bz);
-            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, best));
+            const float tn = fmax3f(tnx, tny, fmaxf(tnz, tmin));
+            const float tf = fmin3f(tfx, tfy, fminf(tfz, best));
             if (tn <= tf * 1.0000004f + 1e-30f) hits |= 1u << k;
         }
         const unsigned imask = w[3] >> 24;

@@ -49,8 +49,15 @@ std::string flatten_tree(const BinaryTree& tree, const float* vertices, int64_t 
 // an SAH-optimal choice of each wide node's children among its binary descendants,
 // octant slot assignment and outward-rounded 8-bit child boxes.  c_tri: the cost of a
 // triangle test relative to a wide-node visit.
+#ifndef MCRT_WIDE_CTRI
+#define MCRT_WIDE_CTRI 0.4f
+#endif
 std::string build_wide(const BinaryTree& tree, const float* vertices, int64_t num_tris, FlatBVH& out,
-                       float c_tri = 0.4f);
+                       float c_tri = MCRT_WIDE_CTRI);
+// Whether this build's FAST traversal walks the eight-child tree (device.cuh, MCRT_FAST_WIDE);
+// scenes then carry it, else the two-child FastNode tree only.
+bool fast_layout_wide();
+
 // Checks every index a traversal of the eight-child layout follows (child blocks, leaf
 // triangle ranges, primitive ids) and the tree depth; an empty string when all are valid.
 std::string validate_wide(const std::vector<WideNode>& nodes, const std::vector<float4>& tris, int64_t num_prims,

@@ -2101,6 +2101,8 @@ int validate_job(const mcrt_scene* s, const mcrt_camera* c, const mcrt_render_pa
 
 int set_error(int code, const std::string& msg) { return fail(code, msg); }
 
+bool fast_layout_wide() { return MCRT_FAST_WIDE != 0; }
+
 const SceneView& scene_view(const mcrt_scene* s) { return s->view; }
 int              scene_device(const mcrt_scene* s) { return s->device; }
 int              scene_stack_depth(const mcrt_scene* s, int traverse) { return stack_depth(s, traverse); }

@@ -61,7 +61,10 @@ struct __align__(32) WideNode
     int4   w2, w3, w4;
     int4   w5;
 };
-constexpr int kWideMaxLeafTris = 4;   // triangles per leaf child
+#ifndef MCRT_WIDE_LEAF
+#define MCRT_WIDE_LEAF 4
+#endif
+constexpr int kWideMaxLeafTris = MCRT_WIDE_LEAF;  // triangles per leaf child
 constexpr int kWideMaxNodeTris = 32;  // triangles per node (the hit mask of a node's leaves)
 
 // inner: a = left, b = (right << 2) | split_axis;  leaf: a = ~ref_begin, b = ref_count

@@ -149,10 +149,14 @@ std::string validate(const HostScene& hs, int64_t num_tris)
         const int32_t p = ibits(r.lo.w);
         if (p < 0 || p >= num_tris) return "reference primitive out of range";
     }
-    int wide_depth = 0;
-    std::string werr = validate_wide(hs.bvh.wide_nodes, hs.bvh.wide_tris, num_tris, &wide_depth);
-    if (!werr.empty()) return werr;
-    if (wide_depth != hs.bvh.wide_depth) return "wide BVH depth does not match the header";
+    if (fast_layout_wide() && hs.bvh.wide_nodes.empty()) return "written for the two-child traversal layout";
+    if (!hs.bvh.wide_nodes.empty())
+    {
+        int         wide_depth = 0;
+        std::string werr = validate_wide(hs.bvh.wide_nodes, hs.bvh.wide_tris, num_tris, &wide_depth);
+        if (!werr.empty()) return werr;
+        if (wide_depth != hs.bvh.wide_depth) return "wide BVH depth does not match the header";
+    }
     const int64_t mats = static_cast<int64_t>(hs.materials.size());
     for (size_t k = 0; k < hs.prim_shade.size(); k += 3)
     {
@@ -345,7 +349,7 @@ extern "C" int mcrt_scene_load(const char* path, uint64_t expected_hash, mcrt_sc
         hs.bvh.wide_depth = hd.wide_depth;
         if (hs.env_w < 0 || hs.env_h < 0 ||
             hs.env_rgb.size() != static_cast<size_t>(hs.env_w) * static_cast<size_t>(hs.env_h) ||
-            hs.bvh.fast_nodes.empty() || hs.bvh.wide_nodes.empty() || hs.materials.empty())
+            hs.bvh.fast_nodes.empty() || hs.materials.empty())
             return set_error(MCRT_ERR_IO, "mcrt_scene_load: inconsistent scene arrays");
         const std::string bad = validate(hs, hd.num_tris);
         if (!bad.empty()) return set_error(MCRT_ERR_IO, "mcrt_scene_load: " + bad);

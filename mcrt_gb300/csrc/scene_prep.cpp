@@ -189,8 +189,11 @@ std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs)
     }
     std::string err = flatten_tree(tree, d.vertices, n, hs.bvh);
     if (!err.empty()) return err;
-    err = build_wide(tree, d.vertices, n, hs.bvh);
-    if (!err.empty()) return err;
+    if (fast_layout_wide())
+    {
+        err = build_wide(tree, d.vertices, n, hs.bvh);
+        if (!err.empty()) return err;
+    }
 
     // per-primitive vertices and shading normals
     hs.prim_verts.resize(3 * n);

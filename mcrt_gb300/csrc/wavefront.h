@@ -36,11 +36,17 @@ constexpr int kSmallStack = 32;
 // caps them at 56 registers, so 9 blocks (36 warps) fit an SM.  Measured on the cfg1 frame:
 // 8 blocks (64 registers) 52.6 / 59.9 ms extend / connect, 9 blocks 52.2 / 56.7, 10 blocks
 // (48 registers, spills) 54.4 / 57.0.
-constexpr int kTraceMinBlocks = 9;
+#ifndef MCRT_TRACE_MIN_BLOCKS
+#define MCRT_TRACE_MIN_BLOCKS 9
+#endif
+constexpr int kTraceMinBlocks = MCRT_TRACE_MIN_BLOCKS;
 // The any-hit next-event kernel under MCRT_VARIANT_REGCAP: 48 registers, 10 blocks per SM.
 // Next-event stage per cfg1 frame: 9 blocks 37.5 ms, 10 blocks 36.5, 12 blocks (40
 // registers, spills) 38.8.
-constexpr int kAnyHitMinBlocks = 10;
+#ifndef MCRT_ANYHIT_MIN_BLOCKS
+#define MCRT_ANYHIT_MIN_BLOCKS 10
+#endif
+constexpr int kAnyHitMinBlocks = MCRT_ANYHIT_MIN_BLOCKS;
 constexpr int kMaxDepth = 62;
 constexpr int64_t kMaxQueue = int64_t(1) << 27;     // rays per queue (result indices stay in int)
 // Streaming schedule default: 64 M rays (49 GB of queues).  Per cfg1 frame (67 M paths):

@@ -47,8 +47,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(LIB_DIR, exist_ok=True)
-    # MCRT_NVCC_DEFINES: extra -D options for the CUDA sources (e.g. -DMCRT_FAST_WIDE=0 builds
-    # the two-child FAST traversal); a change of them rebuilds everything
+    # MCRT_NVCC_DEFINES: extra -D options for all sources (e.g. -DMCRT_FAST_WIDE=0 builds the
+    # two-child FAST traversal); a change of them rebuilds everything
     defines = os.environ.get("MCRT_NVCC_DEFINES", "").split()
     if any(not d.startswith("-D") for d in defines):
         raise ValueError("MCRT_NVCC_DEFINES takes -D options only")
@@ -75,7 +75,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-pthread",
-                         f"-I{cuda}/include", "-c", s, "-o", o])
+                         f"-I{cuda}/include"] + defines + ["-c", s, "-o", o])
 
     def run(cmd):
         if verbose:
