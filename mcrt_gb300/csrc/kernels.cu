@@ -1,7 +1,7 @@
 // CUDA kernels (sm_103a) and the C ABI of mcrt_gb300.h.
 //
 // Kernels:
-//   k_trace<ANY, MODE>   batch closest/any-hit queries (SceneBVH::intersect / occluded)
+//   k_trace<ANY, MODE, STACK, MINB>  batch closest/any-hit queries (SceneBVH::intersect / occluded)
 //   wavefront iterations (wavefront.h; all graph-capturable: every count is read from
 //   device memory, grids are fixed):
 //     k_render_begin, k_wave_next, k_iter_begin   counters and admission
@@ -40,18 +40,30 @@ namespace mcrt {
 // ---------------------------------------------------------------------------
 // batch trace
 // ---------------------------------------------------------------------------
-template <bool ANY, int MODE>
-__global__ void __launch_bounds__(kTraceBlock) k_trace(SceneView s, const float4* __restrict__ rays, int64_t n,
-                                                       float4* __restrict__ hits, int* __restrict__ occ, int* err)
+// Each warp takes the next 32 consecutive rays from a counter until the batch is done (the
+// wavefront traversal kernels' warp batch fetch); STACK / MINB as the wavefront's builds:
+// 32-entry stacks when the tree is shallow enough, registers capped for MINB blocks per SM
+// in FAST mode (MODE 0, a build without the reference traversal), the general build in REF
+// mode (MODE 1).
+template <bool ANY, int MODE, int STACK, int MINB>
+__global__ void __launch_bounds__(kTraceBlock, MINB)
+    k_trace(SceneView s, const float4* __restrict__ rays, int64_t n, float4* __restrict__ hits, int* __restrict__ occ,
+            int* err, unsigned long long* fetch)
 {
-    __shared__ int stack[kStack * kTraceBlock];
+    __shared__ int stack[STACK * kTraceBlock];
     int*           st = stack + threadIdx.x;
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    const int      lane = threadIdx.x & 31;
+    while (true)
     {
-        float4 a = rays[2 * i], b = rays[2 * i + 1];
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(fetch, 32ull);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if (b >= static_cast<unsigned long long>(n)) break;
+        const int64_t i = static_cast<int64_t>(b) + lane;
+        if (i >= n) continue;
+        float4 a = rays[2 * i], d = rays[2 * i + 1];
         Hit    h;
-        bool   any = trace_ray<ANY, kStack>(s, MODE, xyz(a), xyz(b), a.w, b.w, st, kTraceBlock, h, err);
+        bool any = trace_ray<ANY, STACK, false, MODE == 1>(s, MODE, xyz(a), xyz(d), a.w, d.w, st, kTraceBlock, h, err);
         if (ANY)
             occ[i] = any ? 1 : 0;
         else
@@ -1049,6 +1061,13 @@ DeviceWorkspace& device_workspace(int device)
 
 }  // namespace
 
+struct TraceStatus
+{
+    int                err;
+    int                pad;
+    unsigned long long fetch;
+};
+
 struct mcrt_scene
 {
     SceneView          view{};
@@ -1061,9 +1080,10 @@ struct mcrt_scene
     MaterialGPU*       d_materials = nullptr;
     std::vector<int64_t> array_bytes;  // bytes of each uploaded array, in upload order
     uint64_t             desc_hash = 0;  // of the description the scene was built from
-    // error word of the batch-trace calls, one per CUDA stream: calls on one stream run in
-    // order, and calls on different streams (from different host threads) do not share one
-    std::unordered_map<void*, int*> err_by_stream;
+    // error word and ray counter of the batch-trace calls, one pair per CUDA stream: calls
+    // on one stream run in order, and calls on different streams (from different host
+    // threads) do not share one
+    std::unordered_map<void*, TraceStatus*> err_by_stream;
     std::mutex         mu;
 };
 
@@ -2208,13 +2228,13 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
         d_rays = static_cast<const float4*>(tmp_rays);
         d_out = tmp_out;
     }
-    int* d_err = nullptr;
+    TraceStatus* d_status = nullptr;
     {
         std::lock_guard<std::mutex> lock(s->mu);
-        int*&                       slot = s->err_by_stream[stream];
+        TraceStatus*&               slot = s->err_by_stream[stream];
         if (!slot)
         {
-            cudaError_t e = cudaMalloc(&slot, sizeof(int));
+            cudaError_t e = cudaMalloc(&slot, sizeof(TraceStatus));
             if (e != cudaSuccess)
             {
                 slot = nullptr;
@@ -2224,29 +2244,27 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
                 return fail(MCRT_ERR_OUT_OF_MEMORY, "trace error word allocation failed");
             }
         }
-        d_err = slot;
+        d_status = slot;
     }
-    CK(cudaMemsetAsync(d_err, 0, sizeof(int), st));
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace<false, 0>, kTraceBlock, 0);
-    int64_t want = (n + kTraceBlock - 1) / kTraceBlock;
-    int     grid = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(num_sms()) * std::max(occ, 1)));
-    float4* hits = static_cast<float4*>(d_out);
-    int*    o = static_cast<int*>(d_out);
-    if (any)
-    {
-        if (traverse == MCRT_TRAVERSE_REF)
-            k_trace<true, 1><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, nullptr, o, d_err);
-        else
-            k_trace<true, 0><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, nullptr, o, d_err);
-    }
+    CK(cudaMemsetAsync(d_status, 0, sizeof(TraceStatus), st));
+    int*                d_err = &d_status->err;
+    unsigned long long* d_fetch = &d_status->fetch;
+    float4*             hits = static_cast<float4*>(d_out);
+    int*                o = static_cast<int*>(d_out);
+    const bool          small = stack_depth(s, traverse) + 2 < kSmallStack;
+    auto launch = [&](auto kernel) {
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kTraceBlock, 0);
+        const int64_t want = (n + kTraceBlock - 1) / kTraceBlock;
+        const int grid = static_cast<int>(std::min<int64_t>(want, static_cast<int64_t>(num_sms()) * std::max(occ, 1)));
+        kernel<<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, hits, o, d_err, d_fetch);
+    };
+    if (traverse == MCRT_TRAVERSE_REF)
+        any ? launch(k_trace<true, 1, kStack, 1>) : launch(k_trace<false, 1, kStack, 1>);
+    else if (small)
+        any ? launch(k_trace<true, 0, kSmallStack, kAnyHitMinBlocks>) : launch(k_trace<false, 0, kSmallStack, kTraceMinBlocks>);
     else
-    {
-        if (traverse == MCRT_TRAVERSE_REF)
-            k_trace<false, 1><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, hits, nullptr, d_err);
-        else
-            k_trace<false, 0><<<grid, kTraceBlock, 0, st>>>(s->view, d_rays, n, hits, nullptr, d_err);
-    }
+        any ? launch(k_trace<true, 0, kStack, kAnyHitMinBlocks>) : launch(k_trace<false, 0, kStack, kTraceMinBlocks>);
     CK(cudaGetLastError());
     int herr = 0;
     if (ptr_mode != MCRT_PTR_DEVICE) CK(cudaMemcpyAsync(out, tmp_out, out_bytes, cudaMemcpyDeviceToHost, st));
