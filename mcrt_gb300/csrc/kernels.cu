@@ -1080,9 +1080,9 @@ struct mcrt_scene
     MaterialGPU*       d_materials = nullptr;
     std::vector<int64_t> array_bytes;  // bytes of each uploaded array, in upload order
     uint64_t             desc_hash = 0;  // of the description the scene was built from
-    // error word and ray counter of the batch-trace calls, one pair per CUDA stream: calls
-    // on one stream run in order, and calls on different streams (from different host
-    // threads) do not share one
+    // error word and ray counter of the batch-trace calls on device buffers, one pair per
+    // CUDA stream: calls on one stream run in order, and calls on different streams (from
+    // different host threads) do not share one
     std::unordered_map<void*, TraceStatus*> err_by_stream;
     std::mutex         mu;
 };
@@ -2215,10 +2215,16 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
     void*         tmp_rays = nullptr;
     void*         tmp_out = nullptr;
     size_t        out_bytes = static_cast<size_t>(n) * (any ? sizeof(int) : sizeof(float4));
+    // The kernel's error word and ray counter (TraceStatus): with host buffers, in the
+    // call's own temporary allocation, so calls that share a stream from several host
+    // threads (SceneBVH's one-ray queries from OpenMP threads on the default stream) never
+    // share a counter; with device buffers, one per stream (one host thread per stream).
+    const size_t  status_off = (out_bytes + 15) & ~static_cast<size_t>(15);
+    TraceStatus*  d_status = nullptr;
     if (ptr_mode != MCRT_PTR_DEVICE)
     {
         CK(cudaMalloc(&tmp_rays, sizeof(mcrt_ray) * n));
-        cudaError_t e = cudaMalloc(&tmp_out, out_bytes);
+        cudaError_t e = cudaMalloc(&tmp_out, status_off + sizeof(TraceStatus));
         if (e != cudaSuccess)
         {
             cudaFree(tmp_rays);
@@ -2227,8 +2233,9 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
         CK(cudaMemcpyAsync(tmp_rays, rays, sizeof(mcrt_ray) * n, cudaMemcpyHostToDevice, st));
         d_rays = static_cast<const float4*>(tmp_rays);
         d_out = tmp_out;
+        d_status = reinterpret_cast<TraceStatus*>(static_cast<char*>(tmp_out) + status_off);
     }
-    TraceStatus* d_status = nullptr;
+    else
     {
         std::lock_guard<std::mutex> lock(s->mu);
         TraceStatus*&               slot = s->err_by_stream[stream];
@@ -2239,9 +2246,7 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
             {
                 slot = nullptr;
                 s->err_by_stream.erase(stream);
-                cudaFree(tmp_rays);
-                cudaFree(tmp_out);
-                return fail(MCRT_ERR_OUT_OF_MEMORY, "trace error word allocation failed");
+                return fail(MCRT_ERR_OUT_OF_MEMORY, "trace status allocation failed");
             }
         }
         d_status = slot;

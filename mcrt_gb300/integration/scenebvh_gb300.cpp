@@ -180,6 +180,11 @@ HitInfo SceneBVH::intersect(const Ray& ray) const
         miss.reset();
         return miss;
     }
+    if (static_cast<size_t>(h.prim) >= m_triangles_ref.size())
+    {
+        std::fprintf(stderr, "mcrt_trace_closest returned primitive %d of %zu\n", h.prim, m_triangles_ref.size());
+        std::abort();
+    }
     const TriangleObject& tri = m_triangles_ref[h.prim];
     HitInfo               isect(h.t, h.u, h.v, tri.normal(h.u, h.v), &tri);
     isect.setPrimitiveID(h.prim);

@@ -97,7 +97,12 @@ def seam_run(cuda_device):
             pytest.fail("the seam build needs the reference sources (a checkout or baseline/_ref)")
     ctx = mp.get_context("spawn")
     with ctx.Pool(1) as pool:
-        return pool.apply(_child, (8, 16, 1024))
+        # a bounded wait: a child that dies (an abort in the backend) must fail the test,
+        # not leave the pool waiting for a result that never comes
+        try:
+            return pool.apply_async(_child, (8, 16, 1024)).get(timeout=900)
+        except mp.TimeoutError:
+            pytest.fail("the seam child process did not finish within 900 s (it may have died)")
 
 
 def test_scenebvh_seam_runs_reference_ray_trace_on_the_gpu(seam_run):

@@ -237,3 +237,26 @@ def test_fast_any_hit_matches_occluded_at_1_3m_triangles(cfg1_hits, cuda_device)
             near_bound = (fx[f"prim_{k}"] >= 0) & (ulp_diff(fx[f"t_{k}"], rays[:, 7]) <= 4)
             unexplained = diff & ~marginal & ~near_bound
             assert unexplained.sum() <= max(2, rays.shape[0] // 5000), f"cfg1/{k}: {unexplained.sum()} of {diff.sum()}"
+
+
+def test_concurrent_host_buffer_calls_on_the_default_stream(cuda_device):
+    """Several host threads tracing with host buffers on the default stream at once (what
+    the SceneBVH backend does under the reference's OpenMP loops): every call gets its own
+    hits, equal to one batched call's."""
+    from concurrent.futures import ThreadPoolExecutor
+    from mcrt_gb300 import TRAVERSE_FAST
+    fx = golden("ref_traverse_cfg0.npz")
+    sc = _scene(fx, "sah")
+    rays = fx["rays_incoherent"][:2048]
+    want = sc.trace_closest(rays, TRAVERSE_FAST)
+    want_occ = sc.trace_any(rays, TRAVERSE_FAST)
+    chunks = [(i, min(i + s, rays.shape[0])) for i, s in zip(range(0, rays.shape[0], 7), [1, 3, 7] * 1000)]
+
+    def one(c):
+        a, b = c
+        return a, b, sc.trace_closest(rays[a:b], TRAVERSE_FAST), sc.trace_any(rays[a:b], TRAVERSE_FAST)
+
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        for a, b, got, occ in ex.map(one, chunks):
+            assert np.array_equal(got.view(np.int32), want[a:b].view(np.int32)), (a, b)
+            assert np.array_equal(occ, want_occ[a:b]), (a, b)
