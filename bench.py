@@ -381,6 +381,29 @@ def bench_cfg3(args):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_ratio_leg(reps=3):
+    """The metric's adjoint/forward ratio on its own workload (cfg3: the Cornell box with 256
+    albedo groups + emission, 512^2, 32 spp, depth 6): wall time of forward + path-replay
+    adjoint over the forward, best of `reps` (the gradient's accuracy is a test)."""
+    import torch
+    from mcrt_gb300 import GpuScene, scenes
+    desc, albedo, emission = scenes.cfg3_scene()
+    cam = scenes.cfg0_camera(512, 512)
+    sc = GpuScene(desc)
+    out = torch.empty((512, 512, 3), device="cuda")
+    dl = torch.randn((512, 512, 3), device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
+    fwd = lambda: sc.render(cam, out=out, spp=32, max_depth=6, seed=3)  # noqa: E731
+    adj = lambda: sc.render_adjoint(cam, 32, 6, dl, albedo.shape[0], 1, seed=3)  # noqa: E731
+    fwd()
+    adj()
+    tf = min(_timed(fwd)[0] for _ in range(reps))
+    ta = min(_timed(adj)[0] for _ in range(reps))
+    sc.close()
+    return {"workload": "cfg3: Cornell box + 256 albedo groups + emission, 512x512, 32 spp, depth 6",
+            "forward_ms": round(tf * 1e3, 2), "adjoint_ms": round(ta * 1e3, 2),
+            "forward_plus_adjoint_over_forward": round((tf + ta) / tf, 3), "target": "<= 3"}
+
+
 def bench_cfg4(args):
     """32 views of the 1.3 M-triangle scene, 256^2, 16 spp, depth 8, 4,096 albedo
     parameters: batched forward + batched adjoint vs 32 sequential forward + adjoint."""
@@ -588,9 +611,10 @@ def main():
     # launches of our kernels inside the timed region
     launches = st_last["kernel_launches"] * args.steps
 
-    trace_leg = None
+    trace_leg = adjoint = None
     if rank == 0 and not args.quick:
         trace_leg = incoherent_trace_leg(sc, dev)
+        adjoint = adjoint_ratio_leg()
 
     cpu = None
     fp64 = None
@@ -647,6 +671,7 @@ def main():
                                   "shade": round(stage_ms[2], 2), "connect": round(stage_ms[3], 2),
                                   "note": "untimed renders with an event pair around every launch"},
             "trace_incoherent": trace_leg,
+            "adjoint_over_forward": adjoint,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},

@@ -2198,6 +2198,27 @@ int mcrt_scene_set_materials(mcrt_scene* s, int32_t n, const mcrt_material* m, v
     return MCRT_OK;
 }
 
+// Device buffer of the host-buffer trace calls of one host thread on one device, kept for
+// the thread's life (1 MB: up to about 20,000 rays per call).
+constexpr size_t kThreadTraceBufferMax = size_t(1) << 20;
+struct ThreadTraceBuffer
+{
+    void*  ptr = nullptr;
+    size_t bytes = 0;
+    ~ThreadTraceBuffer()
+    {
+        if (ptr) cudaFree(ptr);  // at thread exit (an error after the runtime is gone is ignored)
+    }
+};
+
+// this thread's buffer for `device`, or null (device index past the table: no reuse)
+ThreadTraceBuffer* thread_trace_buffer(int device)
+{
+    constexpr int                  kDevices = 64;
+    thread_local ThreadTraceBuffer buffers[kDevices];
+    return device >= 0 && device < kDevices ? &buffers[device] : nullptr;
+}
+
 static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out, bool any, int32_t traverse,
                       int32_t ptr_mode, void* stream)
 {
@@ -2221,14 +2242,39 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
     // share a counter; with device buffers, one per stream (one host thread per stream).
     const size_t  status_off = (out_bytes + 15) & ~static_cast<size_t>(15);
     TraceStatus*  d_status = nullptr;
+    bool          owned = false;  // tmp_rays / tmp_out allocated by this call (freed at its end)
     if (ptr_mode != MCRT_PTR_DEVICE)
     {
-        CK(cudaMalloc(&tmp_rays, sizeof(mcrt_ray) * n));
-        cudaError_t e = cudaMalloc(&tmp_out, status_off + sizeof(TraceStatus));
-        if (e != cudaSuccess)
+        // small requests (the SceneBVH backend's one-ray queries) reuse a buffer kept per
+        // host thread and device: no cudaMalloc / cudaFree (which synchronises the device)
+        // per call
+        const size_t rays_bytes = (sizeof(mcrt_ray) * n + 15) & ~static_cast<size_t>(15);
+        const size_t need = rays_bytes + status_off + sizeof(TraceStatus);
+        ThreadTraceBuffer* tb = thread_trace_buffer(s->device);
+        if (tb && need <= kThreadTraceBufferMax)
         {
-            cudaFree(tmp_rays);
-            return fail(MCRT_ERR_OUT_OF_MEMORY, "trace buffer allocation failed");
+            if (tb->bytes < need)
+            {
+                if (cudaMalloc(&tb->ptr, kThreadTraceBufferMax) != cudaSuccess)
+                {
+                    tb->ptr = nullptr;
+                    return fail(MCRT_ERR_OUT_OF_MEMORY, "trace buffer allocation failed");
+                }
+                tb->bytes = kThreadTraceBufferMax;
+            }
+            tmp_rays = tb->ptr;
+            tmp_out = static_cast<char*>(tb->ptr) + rays_bytes;
+        }
+        else
+        {
+            CK(cudaMalloc(&tmp_rays, sizeof(mcrt_ray) * n));
+            cudaError_t e = cudaMalloc(&tmp_out, status_off + sizeof(TraceStatus));
+            if (e != cudaSuccess)
+            {
+                cudaFree(tmp_rays);
+                return fail(MCRT_ERR_OUT_OF_MEMORY, "trace buffer allocation failed");
+            }
+            owned = true;
         }
         CK(cudaMemcpyAsync(tmp_rays, rays, sizeof(mcrt_ray) * n, cudaMemcpyHostToDevice, st));
         d_rays = static_cast<const float4*>(tmp_rays);
@@ -2275,8 +2321,11 @@ static int trace_impl(mcrt_scene* s, const mcrt_ray* rays, int64_t n, void* out,
     if (ptr_mode != MCRT_PTR_DEVICE) CK(cudaMemcpyAsync(out, tmp_out, out_bytes, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    cudaFree(tmp_rays);
-    cudaFree(tmp_out);
+    if (owned)
+    {
+        cudaFree(tmp_rays);
+        cudaFree(tmp_out);
+    }
     if (herr & kErrStack) return fail(MCRT_ERR_STACK_OVERFLOW, "traversal stack overflow");
     return MCRT_OK;
 }
