@@ -1,4 +1,5 @@
 """Hit parity of the CUDA traversal against the reference SplitBVH, through the C ABI."""
+import os
 import numpy as np
 import pytest
 
@@ -260,3 +261,45 @@ def test_concurrent_host_buffer_calls_on_the_default_stream(cuda_device):
         for a, b, got, occ in ex.map(one, chunks):
             assert np.array_equal(got.view(np.int32), want[a:b].view(np.int32)), (a, b)
             assert np.array_equal(occ, want_occ[a:b]), (a, b)
+
+
+def test_ref_mode_bit_exact_at_1_3m_triangles(cfg1_hits, cuda_device):
+    """REF mode at full scale: the reference's own SplitBVH of the 1,310,722 triangles,
+    built here by the reference's code (oracle/_ref, about a minute), traversed on the GPU in
+    the reference's order and arithmetic: prim, t, u and v identical to the reference's
+    SplitBVH::intersect on every ray of the four classes, and prim and t identical to the
+    fixture's (made on another machine from the same sources)."""
+    import ctypes
+    from mcrt_gb300 import GpuScene, TRAVERSE_REF
+    from mcrt_gb300.scene import DIFF, Material, SceneDesc
+    from oracle.oracle import load_reference, ptr
+    ref = load_reference()
+    if ref is None:
+        pytest.skip("the reference build (oracle/_ref) is not present")
+    fx, verts, _ = cfg1_hits
+    h = ref.ref_bvh_create(ptr(verts), verts.shape[0], 0)
+    try:
+        nn, nr = ctypes.c_int(), ctypes.c_int()
+        ref.ref_bvh_dump_sizes(h, ctypes.byref(nn), ctypes.byref(nr))
+        tree = dict(node_box=np.zeros((nn.value, 6), np.float32), node_info=np.zeros((nn.value, 6), np.int32),
+                    ref_prim=np.zeros(nr.value, np.int32), ref_box=np.zeros((nr.value, 6), np.float32))
+        ref.ref_bvh_dump(h, ptr(tree["node_box"]), ptr(tree["node_info"]), ptr(tree["ref_prim"]), ptr(tree["ref_box"]))
+        sc = GpuScene(SceneDesc(verts, np.zeros(verts.shape[0], np.int32), [Material(DIFF)]), builder="external",
+                      external_tree=tree)
+        for k in CFG1_SETS:
+            rays = np.ascontiguousarray(fx[f"rays_{k}"])
+            n = rays.shape[0]
+            t, p, u, v = (np.zeros(n, np.float32), np.zeros(n, np.int32), np.zeros(n, np.float32),
+                          np.zeros(n, np.float32))
+            ref.ref_bvh_intersect(h, ptr(rays), n, ptr(t), ptr(p), ptr(u), ptr(v), os.cpu_count() or 1)
+            out = sc.trace_closest(rays, TRAVERSE_REF)
+            prim = out[:, 3].view(np.int32)
+            assert np.array_equal(prim, p), f"cfg1/{k}: {np.sum(prim != p)} prim mismatches"
+            hit = p >= 0
+            for c, want in ((0, t), (1, u), (2, v)):
+                assert np.array_equal(out[hit, c].view(np.int32), want[hit].view(np.int32)), f"cfg1/{k}: column {c}"
+            assert np.array_equal(p, fx[f"prim_{k}"]), f"cfg1/{k}: the reference's hits differ from the fixture's"
+            assert np.array_equal(t[hit].view(np.int32), fx[f"t_{k}"][hit].view(np.int32))
+        sc.close()
+    finally:
+        ref.ref_bvh_destroy(h)
