@@ -326,3 +326,21 @@ def test_phong_crn_matches_float_oracle(cuda_device):
     ref = OracleScene(desc, 32).render(cam.as_array(), 32, 32, 16, 8, 3, seed=9)
     _crn_compare(gpu, ref["mean"].astype(np.float32), "phong")
     assert abs(st["rays"] - ref["rays"]) <= 0.01 * ref["rays"]
+
+
+def test_scene_built_through_the_mcrt_api_renders_the_same_image(cuda_device):
+    """The reference's Cornell box built with MCRT's calls (mcrt_gb300.mcrt_scene: Scene::add,
+    todo_addMaterial, setCamera, finalize) renders bit for bit the image of the same scene
+    described directly."""
+    from conftest import golden
+    from mcrt_gb300.mcrt_scene import Material, Scene, TriangleObject, todo_addMaterial
+    fx, desc, cam, _ = _reference_cornell_scene()
+    sc = Scene()
+    for v, t, c in zip(fx["verts"], fx["mat_types"], fx["mat_colors"]):
+        m = todo_addMaterial(Material(tuple(float(x) for x in c), 0.0, int(t)))
+        sc.add(TriangleObject(tuple(v[0:3]), tuple(v[3:6]), tuple(v[6:9])), m)
+    sc.setCamera(cam.origin, cam.target, cam.width, cam.height, cam.fov_y)
+    from mcrt_gb300 import GpuScene
+    a, _ = sc.finalize().render(sc.camera(), spp=8, max_depth=10, seed=5)
+    b, _ = GpuScene(desc).render(cam, spp=8, max_depth=10, seed=5)
+    np.testing.assert_array_equal(a, b)
