@@ -83,8 +83,11 @@ typedef struct mcrt_bvh_tree {
     const float*   ref_box;
 } mcrt_bvh_tree;
 
-#define MCRT_BUILD_SAH 0      /* the library's own binned-SAH builder */
-#define MCRT_BUILD_EXTERNAL 1 /* use desc->external_tree */
+#define MCRT_BUILD_SAH 0       /* the library's own binned-SAH builder */
+#define MCRT_BUILD_EXTERNAL 1  /* use desc->external_tree */
+#define MCRT_BUILD_SAH_SPLIT 2 /* the library's builder with spatial splits (references straddling a
+                                  split plane duplicated with clipped boxes, as the reference's
+                                  SplitBVH, splitbvh.cpp:664-1408) */
 
 typedef struct mcrt_scene_desc {
     int64_t              num_triangles;
@@ -222,6 +225,10 @@ int mcrt_vertex_alpha(const float* vertices, const float* normals, int64_t num_t
  * (splitbvh.cpp:1410-1625) for callers that build trees themselves. */
 int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int32_t leaf_size, int32_t* num_nodes,
                    int32_t* num_refs, float* node_box, int32_t* node_info, int32_t* ref_prim, float* ref_box);
+/* The same with spatial splits (MCRT_BUILD_SAH_SPLIT): replaces SplitBVH::build
+ * (splitbvh.cpp:1410-1625, spatial splitters :664-1408); refs may repeat a primitive. */
+int mcrt_build_bvh_split(const float* vertices, int64_t num_triangles, int32_t leaf_size, int32_t* num_nodes,
+                         int32_t* num_refs, float* node_box, int32_t* node_info, int32_t* ref_prim, float* ref_box);
 
 /* Scene inputs from the reference's file formats (host only, no GPU needed).
  * mcrt_mesh_load_obj: the triangles Scene::loadModel(path, transform, mat) adds

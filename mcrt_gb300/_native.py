@@ -41,6 +41,7 @@ SCHEDULE_STREAM = 0
 SCHEDULE_WAVES = 1
 BUILD_SAH = 0
 BUILD_EXTERNAL = 1
+BUILD_SAH_SPLIT = 2
 MAT_CONSISTENT = 0x100
 
 
@@ -122,6 +123,8 @@ EXPORTS = {
     "mcrt_vertex_alpha": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),
     "mcrt_build_bvh": (c_int32, [c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32), ctypes.POINTER(c_int32),
                                  c_void_p, c_void_p, c_void_p, c_void_p]),
+    "mcrt_build_bvh_split": (c_int32, [c_void_p, c_int64, c_int32, ctypes.POINTER(c_int32),
+                                       ctypes.POINTER(c_int32), c_void_p, c_void_p, c_void_p, c_void_p]),
     "mcrt_scene_desc_hash": (c_int32, [ctypes.POINTER(SceneDesc), ctypes.POINTER(ctypes.c_uint64)]),
     "mcrt_mesh_load_obj": (c_int32, [ctypes.c_char_p, c_void_p, ctypes.POINTER(c_int64), c_void_p, c_void_p,
                                      c_void_p]),

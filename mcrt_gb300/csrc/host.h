@@ -29,6 +29,10 @@ constexpr int kDefaultLeafSize = 2;
 // Multithreaded over subtrees.  Leaves reference contiguous runs of ref_prim.
 void build_sah_tree(const float* vertices, int64_t num_tris, int leaf_size, BinaryTree& out);
 
+// The same with spatial splits (sbvh_build.cpp): references straddling a split plane are
+// duplicated with clipped boxes.  Leaves reference contiguous runs of ref_prim.
+void build_split_tree(const float* vertices, int64_t num_tris, int leaf_size, BinaryTree& out);
+
 struct FlatBVH
 {
     std::vector<FastNode> fast_nodes;

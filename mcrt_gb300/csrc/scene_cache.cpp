@@ -365,9 +365,9 @@ extern "C" int mcrt_scene_load(const char* path, uint64_t expected_hash, mcrt_sc
     }
 }
 
-extern "C" int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int32_t leaf_size, int32_t* num_nodes,
-                              int32_t* num_refs, float* node_box, int32_t* node_info, int32_t* ref_prim,
-                              float* ref_box)
+static int build_bvh_impl(bool split, const float* vertices, int64_t num_triangles, int32_t leaf_size,
+                          int32_t* num_nodes, int32_t* num_refs, float* node_box, int32_t* node_info, int32_t* ref_prim,
+                          float* ref_box)
 {
     if (!vertices || num_triangles <= 0 || !num_nodes || !num_refs)
         return set_error(MCRT_ERR_INVALID_ARGUMENT, "mcrt_build_bvh: null argument or no triangles");
@@ -376,7 +376,10 @@ extern "C" int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int3
     try
     {
         BinaryTree t;
-        build_sah_tree(vertices, num_triangles, leaf_size > 0 ? leaf_size : kDefaultLeafSize, t);
+        if (split)
+            build_split_tree(vertices, num_triangles, leaf_size > 0 ? leaf_size : kDefaultLeafSize, t);
+        else
+            build_sah_tree(vertices, num_triangles, leaf_size > 0 ? leaf_size : kDefaultLeafSize, t);
         const int64_t nodes = static_cast<int64_t>(t.node_info.size() / 6);
         const int64_t refs = static_cast<int64_t>(t.ref_prim.size());
         if (nodes > INT32_MAX || refs > INT32_MAX) return set_error(MCRT_ERR_INVALID_ARGUMENT, "tree too large");
@@ -402,4 +405,20 @@ extern "C" int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int3
     {
         return set_error(MCRT_ERR_INTERNAL, "unexpected exception in mcrt_build_bvh");
     }
+}
+
+extern "C" int mcrt_build_bvh(const float* vertices, int64_t num_triangles, int32_t leaf_size, int32_t* num_nodes,
+                              int32_t* num_refs, float* node_box, int32_t* node_info, int32_t* ref_prim,
+                              float* ref_box)
+{
+    return build_bvh_impl(false, vertices, num_triangles, leaf_size, num_nodes, num_refs, node_box, node_info,
+                          ref_prim, ref_box);
+}
+
+extern "C" int mcrt_build_bvh_split(const float* vertices, int64_t num_triangles, int32_t leaf_size,
+                                    int32_t* num_nodes, int32_t* num_refs, float* node_box, int32_t* node_info,
+                                    int32_t* ref_prim, float* ref_box)
+{
+    return build_bvh_impl(true, vertices, num_triangles, leaf_size, num_nodes, num_refs, node_box, node_info,
+                          ref_prim, ref_box);
 }

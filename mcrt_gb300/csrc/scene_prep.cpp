@@ -177,11 +177,14 @@ std::string prepare_scene(const mcrt_scene_desc& d, HostScene& hs)
         tree.ref_box.assign(t->ref_box, t->ref_box + 6 * static_cast<size_t>(t->num_refs));
         tree.root = 0;
     }
-    else if (d.builder == MCRT_BUILD_SAH)
+    else if (d.builder == MCRT_BUILD_SAH || d.builder == MCRT_BUILD_SAH_SPLIT)
     {
         int leaf = d.leaf_size > 0 ? d.leaf_size : kDefaultLeafSize;
         if (leaf > 15) return "leaf_size must be <= 15";
-        build_sah_tree(d.vertices, n, leaf, tree);
+        if (d.builder == MCRT_BUILD_SAH)
+            build_sah_tree(d.vertices, n, leaf, tree);
+        else
+            build_split_tree(d.vertices, n, leaf, tree);
     }
     else
     {

@@ -22,7 +22,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["kernels.cu", "noalloc.cu", "film.cu", "probe.cu"]
 CPP_SOURCES = ["bvh_build.cpp", "flatten.cpp", "scene_prep.cpp", "autotune.cpp", "scene_cache.cpp", "ingest.cpp",
-               "wide_build.cpp"]
+               "wide_build.cpp", "sbvh_build.cpp"]
 HEADERS = ["layout.h", "host.h", "device.cuh", "estimator.cuh", "wavefront.h"]
 
 

@@ -140,8 +140,12 @@ def _c_desc(desc: SceneDesc, builder: str = "sah", external_tree: dict | None = 
         d.builder = N.BUILD_EXTERNAL
         d.external_tree = ctypes.pointer(tree)
         keep += [nb, ni, rp, rb, tree]
-    else:
+    elif builder == "sah_split":
+        d.builder = N.BUILD_SAH_SPLIT
+    elif builder == "sah":
         d.builder = N.BUILD_SAH
+    else:
+        raise ValueError(f"unknown builder {builder!r} (sah, sah_split, external)")
     return d, keep
 
 
@@ -185,20 +189,22 @@ def load_envmap_bin(path: str) -> np.ndarray:
     return img
 
 
-def build_bvh(vertices, leaf_size: int = 0) -> dict:
-    """mcrt_build_bvh: the library's binned-SAH tree of (n, 9) triangle vertices, in the
-    form of a reference SplitBVH dump (node_box, node_info, ref_prim, ref_box; root 0)."""
+def build_bvh(vertices, leaf_size: int = 0, split: bool = False) -> dict:
+    """mcrt_build_bvh (split: mcrt_build_bvh_split, with spatial splits): the library's
+    binned-SAH tree of (n, 9) triangle vertices, in the form of a reference SplitBVH dump
+    (node_box, node_info, ref_prim, ref_box; root 0)."""
     lib = N.load()
+    fn = lib.mcrt_build_bvh_split if split else lib.mcrt_build_bvh
     v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
     nn, nr = ctypes.c_int32(), ctypes.c_int32()
-    N.check(lib.mcrt_build_bvh(v.ctypes.data, v.shape[0], int(leaf_size), ctypes.byref(nn), ctypes.byref(nr),
-                               None, None, None, None), "mcrt_build_bvh")
+    N.check(fn(v.ctypes.data, v.shape[0], int(leaf_size), ctypes.byref(nn), ctypes.byref(nr),
+               None, None, None, None), "mcrt_build_bvh")
     nb = np.zeros((nn.value, 6), np.float32)
     ni = np.zeros((nn.value, 6), np.int32)
     rp = np.zeros(nr.value, np.int32)
     rb = np.zeros((nr.value, 6), np.float32)
-    N.check(lib.mcrt_build_bvh(v.ctypes.data, v.shape[0], int(leaf_size), ctypes.byref(nn), ctypes.byref(nr),
-                               nb.ctypes.data, ni.ctypes.data, rp.ctypes.data, rb.ctypes.data), "mcrt_build_bvh")
+    N.check(fn(v.ctypes.data, v.shape[0], int(leaf_size), ctypes.byref(nn), ctypes.byref(nr),
+               nb.ctypes.data, ni.ctypes.data, rp.ctypes.data, rb.ctypes.data), "mcrt_build_bvh")
     return {"node_box": nb, "node_info": ni, "ref_prim": rp, "ref_box": rb}
 
 

@@ -145,6 +145,10 @@ def test_own_builder_sah_cost_against_reference_trees(native):
         ours = build_bvh(g["verts"], leaf_size=4)
         assert sorted(np.unique(ours["ref_prim"])) == list(range(g["verts"].reshape(-1, 9).shape[0]))
         assert sah_cost(ours) <= lim * sah_cost(ref), name
+        # with spatial splits: every triangle referenced, the cost no worse than object splits
+        split = build_bvh(g["verts"], leaf_size=4, split=True)
+        assert sorted(np.unique(split["ref_prim"])) == list(range(g["verts"].reshape(-1, 9).shape[0]))
+        assert sah_cost(split) <= 1.001 * sah_cost(ours), name
 
 
 def test_vertex_alpha_matches_reference_mesh(native):

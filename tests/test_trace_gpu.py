@@ -16,7 +16,7 @@ def _scene(fx, builder):
     desc = fixture_scene(fx)
     if builder == "external":
         return GpuScene(desc, builder="external", external_tree=fixture_tree(fx))
-    return GpuScene(desc)
+    return GpuScene(desc, builder=builder)
 
 
 def _sets(fx):
@@ -55,7 +55,7 @@ def test_ref_mode_occluded_matches_scenebvh(name, cuda_device):
         assert np.array_equal(occ, fx[f"occ_{k}"]), f"{name}/{k}: {np.sum(occ != fx[f'occ_{k}'])} mismatches"
 
 
-@pytest.mark.parametrize("builder", ["external", "sah"])
+@pytest.mark.parametrize("builder", ["external", "sah", "sah_split"])
 @pytest.mark.parametrize("name", FIXTURES)
 def test_fast_mode_nonmarginal(name, builder, cuda_device):
     """Watertight FP32 traversal: same prim and t within 4 ulp on every non-marginal ray."""

@@ -63,11 +63,19 @@ def _check(verts, rays, ref_t, ref_p, t, p, what):
     assert not bad.any(), f"{what}: {bad.sum()} non-marginal mismatches, e.g. ray {np.argmax(bad)}"
 
 
-@pytest.mark.parametrize("builder", ["sah", "external"])
+@pytest.mark.parametrize("builder", ["sah", "external", "sah_split"])
 @pytest.mark.parametrize("name", FIXTURES)
 def test_wide_tree_closest_and_any_hit_on_the_host(name, builder, harness):
+    """sah: the library's builder; external: the reference's SplitBVH tree; sah_split: the
+    library's spatial-split builder, whose clipped reference boxes must still contain the
+    parts of the triangles they stand for (a box clipped too tightly loses hits here)."""
     fx = golden(f"ref_traverse_{name}.npz")
-    tree = fixture_tree(fx) if builder == "external" else None
+    tree = None
+    if builder == "external":
+        tree = fixture_tree(fx)
+    elif builder == "sah_split":
+        from mcrt_gb300.scene import build_bvh
+        tree = build_bvh(fx["verts"], leaf_size=2, split=True)
     for k in TRAVERSE_SETS:
         if f"rays_{k}" not in fx.files:
             continue
