@@ -332,6 +332,7 @@ struct FastTrav
     float3        inv, ood;
     WatertightRay wr;
     float         tmin, best;
+    float         tterm;  // TERM: a hit nearer than this ends the traversal
     Hit           hit;
     int           sp, cur;
 };
@@ -353,9 +354,10 @@ __device__ __forceinline__ void fast_begin(FastTrav& r, float3 o, float3 d, floa
 }
 
 // Inner nodes down to the next leaf, that leaf's triangles, then the next node from the
-// stack.  Returns true when the traversal is over: stack empty, an any-hit query hit,
-// or the stack overflowed (error bit set, the hit so far kept).
-template <int STACK, bool COUNT>
+// stack.  Returns true when the traversal is over: stack empty, an any-hit query hit, a
+// TERM query hit nearer than r.tterm, or the stack overflowed (error bit set, the hit so
+// far kept).
+template <int STACK, bool COUNT, bool TERM = false>
 __device__ __forceinline__ bool fast_step(FastTrav& r, const FastNode* nodes, const float4* tris, bool any, int* stack,
                                           int stride, int* err, TraceCount* cnt)
 {
@@ -428,7 +430,7 @@ __device__ __forceinline__ bool fast_step(FastTrav& r, const FastNode* nodes, co
                 r.best = t;
                 r.hit.t = t;  // u, v: recomputed for the final hit only (refine_hit)
                 r.hit.prim = __float_as_int(a.w);
-                if (any) return true;
+                if (any || (TERM && t < r.tterm)) return true;
             }
         }
         r.cur = stack[r.sp * stride];
@@ -437,13 +439,15 @@ __device__ __forceinline__ bool fast_step(FastTrav& r, const FastNode* nodes, co
     return r.cur == kSentinel;
 }
 
-template <bool ANY, int STACK, bool COUNT = false>
+template <bool ANY, int STACK, bool COUNT = false, bool TERM = false>
 __device__ __forceinline__ bool trace_fast(const SceneView& s, float3 o, float3 d, float tmin, float tmax,
-                                           int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr)
+                                           int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr,
+                                           float tterm = 0.f)
 {
     FastTrav r;
     fast_begin(r, o, d, tmin, tmax, stack);
-    while (!fast_step<STACK, COUNT>(r, s.fast_nodes, s.fast_tris, ANY, stack, stride, err, cnt))
+    r.tterm = tterm;
+    while (!fast_step<STACK, COUNT, TERM>(r, s.fast_nodes, s.fast_tris, ANY, stack, stride, err, cnt))
     {
     }
     hit = r.hit;
@@ -816,15 +820,22 @@ MCRT_HDI void refine_hit(const SceneView& s, float3 o, float3 d, float tmin, Hit
 // REFM = false: a build for jobs that all traverse in FAST mode; without the reference
 // traversal in the same kernel the fast one needs fewer registers (the any-hit kernel at
 // 48 registers: 8 B of spills instead of 52).
-template <bool ANY, int STACK, bool COUNT = false, bool REFM = true>
+// TERM: a closest-hit query that only asks whether the ray reaches an emitter, and `tterm`
+// a distance no emitter hit can lie below (emitter_span): the FAST traversal stops at a
+// nearer hit and reports no hit, which is the answer the full query gives the caller (its
+// closest hit, nearer still, is no emitter).  The reference-order traversal and the wide
+// one run the full query.
+template <bool ANY, int STACK, bool COUNT = false, bool REFM = true, bool TERM = false>
 __device__ __forceinline__ bool trace_ray(const SceneView& s, int mode, float3 o, float3 d, float tmin, float tmax,
-                                          int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr)
+                                          int* stack, int stride, Hit& hit, int* err, TraceCount* cnt = nullptr,
+                                          float tterm = 0.f)
 {
     if (REFM && mode == 1) return trace_ref<ANY, STACK>(s, o, d, tmin, tmax, stack, stride, hit, err);
 #if MCRT_FAST_WIDE
     bool found = trace_wide<ANY, STACK, COUNT>(s, o, d, tmin, tmax, stack, stride, hit, err, cnt);
 #else
-    bool found = trace_fast<ANY, STACK, COUNT>(s, o, d, tmin, tmax, stack, stride, hit, err, cnt);
+    bool found = trace_fast<ANY, STACK, COUNT, TERM>(s, o, d, tmin, tmax, stack, stride, hit, err, cnt, tterm);
+    if (TERM && found && hit.t < tterm) return false;
 #endif
     if (!ANY && found) refine_hit(s, o, d, tmin, hit);
     return found;

@@ -27,7 +27,35 @@ struct NeeRay
     float4 val;
     int    type;
     int    light;
+    float  tterm;  // closest-hit rays: a hit nearer than this cannot be an emitter (-inf: none)
 };
+
+// The part [t0, t1] of the ray o + t d (d unit length) inside the bounding box of the
+// emitter triangles, widened by the scene's margin plus 1e-3 of the origin's largest
+// coordinate so that every hit the traversal reports on an emitter lies inside it.  False
+// when the ray cannot reach an emitter: then the closest hit, whatever it is, is not one.
+__device__ __forceinline__ bool emitter_span(const SceneView& S, float3 o, float3 d, float& t0, float& t1)
+{
+    const float pad = S.light_pad + 1e-3f * fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
+    t0 = -__int_as_float(0x7f800000);
+    t1 = __int_as_float(0x7f800000);
+    const float lo[3] = {S.light_lo.x - pad, S.light_lo.y - pad, S.light_lo.z - pad};
+    const float hi[3] = {S.light_hi.x + pad, S.light_hi.y + pad, S.light_hi.z + pad};
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        if (dd[a] == 0.f)
+        {
+            if (oo[a] < lo[a] || oo[a] > hi[a]) return false;
+            continue;
+        }
+        const float ta = (lo[a] - oo[a]) / dd[a], tb = (hi[a] - oo[a]) / dd[a];
+        t0 = fmaxf(t0, fminf(ta, tb));
+        t1 = fminf(t1, fmaxf(ta, tb));
+    }
+    return t0 <= t1;
+}
 
 // emission picked up when the extension ray misses or hits an emitter
 // LIGHTS: the light kinds a build handles (1 environment, 2 area lights, 3 both); the
@@ -95,11 +123,15 @@ __device__ __forceinline__ int make_nee(const SceneView& S, const Mat& m, float3
     if ((LIGHTS & 2) && S.light_area > 0.f)
     {
         // BSDF sample, MIS against the area lights (demo_pt.cpp:593-614)
+        // Only a ray that meets the emitters' box can contribute: the others are not traced,
+        // and the traced ones end at the box (a farther hit is no emitter) and stop at a hit
+        // before it (the closest hit is then no emitter either)
         BsdfSample bs = bsdf_sample(m, wi, ns, u[D_AREA_BSDF_0], u[D_AREA_BSDF_1]);
-        if (maxc(bs.weight) > 0.f)
+        float      e0, e1;
+        if (maxc(bs.weight) > 0.f && emitter_span(S, phit, bs.wo, e0, e1) && e1 >= kEpsRay)
         {
             float3 val = T * bs.weight;
-            out[k++] = NeeRay{bs.wo, inf, make_float4(val.x, val.y, val.z, bs.pdf), NEE_AREA_BSDF, 0};
+            out[k++] = NeeRay{bs.wo, e1, make_float4(val.x, val.y, val.z, bs.pdf), NEE_AREA_BSDF, 0, e0};
         }
         // light sample (demo_pt.cpp:618-641; Scene::sampleLightArea, scene.cpp:298-343)
         int lo = 0, hi = S.num_lights - 1;
@@ -131,13 +163,15 @@ __device__ __forceinline__ int make_nee(const SceneView& S, const Mat& m, float3
             float  mis = pdfW / (pdfW + pb);
             float3 f = bsdf_eval(m, wi, ns, wo);
             float  cs = fmaxf(dot3(ns, wo), 0.f);
-            if (maxc(f) > 0.f && cs > 0.f)
+            float e0, e1;
+            if (maxc(f) > 0.f && cs > 0.f && emitter_span(S, phit, wo, e0, e1))
             {
                 float3 val = T * (f * (cs / pdfW * mis));
                 // closest hit bounded just past the sampled point: the same answer as the
-                // reference's unbounded query for "did the ray reach emitter `lo`"
+                // reference's unbounded query for "did the ray reach emitter `lo`"; a hit
+                // before the emitters' box ends the query (the ray is blocked)
                 out[k++] = NeeRay{wo, sqrtf(dist2) * 1.001f + kEpsRay, make_float4(val.x, val.y, val.z, 0.f),
-                                  NEE_AREA_LIGHT, lo};
+                                  NEE_AREA_LIGHT, lo, e0};
             }
         }
     }

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <mutex>
 #include <new>
 #include <string>
@@ -753,7 +754,8 @@ __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
                     atomicOr(a.err, kErrQueue);
                     break;
                 }
-                a.so[qsel][idx] = make_float4(phit.x, phit.y, phit.z, kEpsRay);
+                // .w: where a closest-hit ray stops at a nearer hit (tmin is kEpsRay for all)
+                a.so[qsel][idx] = make_float4(phit.x, phit.y, phit.z, nee[r].tterm);
                 a.sd[qsel][idx] = make_float4(nee[r].d.x, nee[r].d.y, nee[r].d.z, nee[r].tmax);
                 a.sv[qsel][idx] = nee[r].val;
                 a.sm[qsel][idx] = make_int4(dest + r, nee[r].type | (nee[r].light << 2), pixel, job);
@@ -809,8 +811,8 @@ __global__ void __launch_bounds__(kTraceBlock, (Q == 0 && MINB > 1) ? kAnyHitMin
         float4        o = a.so[Q][k], d = a.sd[Q][k];
         const JobGPU& J = a.jobs[a.sm[Q][k].w];
         Hit           h;
-        bool hit = trace_ray<Q == 0, STACK, COUNT, REFM>(J.scene, J.traverse, xyz(o), xyz(d), o.w, d.w, st,
-                                                         kTraceBlock, h, a.err, &cnt);
+        bool hit = trace_ray<Q == 0, STACK, COUNT, REFM, Q == 1>(J.scene, J.traverse, xyz(o), xyz(d), kEpsRay, d.w,
+                                                                 st, kTraceBlock, h, a.err, &cnt, o.w);
         connect_result<ADJ>(a, G, p, Q, k, hit, h);
     }
     if (COUNT) flush_count(a.stats, 4, cnt);
@@ -930,8 +932,9 @@ __global__ void __launch_bounds__(kAdjBlock) k_adjoint(AdjointArgs a)
                     bool any = nee[r].type == NEE_ENV;
                     bool hh = any ? trace_ray<true, STACK>(S, J.traverse, phit, nee[r].d, kEpsRay, nee[r].tmax, st,
                                                           kAdjBlock, hs, a.err)
-                                  : trace_ray<false, STACK>(S, J.traverse, phit, nee[r].d, kEpsRay, nee[r].tmax, st,
-                                                           kAdjBlock, hs, a.err);
+                                  : trace_ray<false, STACK, false, true, true>(S, J.traverse, phit, nee[r].d, kEpsRay,
+                                                                           nee[r].tmax, st, kAdjBlock, hs, a.err,
+                                                                           nullptr, nee[r].tterm);
                     ++rays;
                     float3 coef;
                     int    emat;
@@ -1985,6 +1988,29 @@ CameraGPU make_camera(const mcrt_camera& c) { return make_camera_impl(c); }
 
 // uploads a prepared scene; the arrays are kept in upload order with their byte counts so
 // the scene can be written to a cache file (scene_to_host)
+// Bounding box of the emitter triangles and its margin: 1e-3 of the box diagonal plus its
+// largest coordinate, far above the rounding of a triangle's hit distance (a few ulp of the
+// vertex and origin coordinates); an empty box when the scene has no emitters.
+static void emitter_box(const HostScene& hs, float3& lo, float3& hi, float& pad)
+{
+    const float inf = std::numeric_limits<float>::infinity();
+    lo = make_float3(inf, inf, inf);
+    hi = make_float3(-inf, -inf, -inf);
+    pad = 0.f;
+    for (const LightGPU& l : hs.lights)
+        for (int c = 0; c < 3; ++c)
+        {
+            const float4 v = hs.prim_verts[3 * static_cast<size_t>(l.prim) + c];
+            lo = make_float3(std::min(lo.x, v.x), std::min(lo.y, v.y), std::min(lo.z, v.z));
+            hi = make_float3(std::max(hi.x, v.x), std::max(hi.y, v.y), std::max(hi.z, v.z));
+        }
+    if (hs.lights.empty()) return;
+    const double dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    const double mag = std::max({std::fabs(lo.x), std::fabs(lo.y), std::fabs(lo.z), std::fabs(hi.x),
+                                 std::fabs(hi.y), std::fabs(hi.z)});
+    pad = static_cast<float>(1e-3 * (std::sqrt(dx * dx + dy * dy + dz * dz) + mag));
+}
+
 int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, mcrt_scene** out)
 {
     mcrt_scene* s = new mcrt_scene();
@@ -2054,6 +2080,7 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
     v.env_guide_c = egc;
     v.num_lights = static_cast<int>(hs.lights.size());
     v.light_area = hs.light_area;
+    emitter_box(hs, v.light_lo, v.light_hi, v.light_pad);
     v.env_w = hs.env_w;
     v.env_h = hs.env_h;
     v.env_norm = hs.env_norm;

@@ -124,6 +124,10 @@ struct SceneView
     const float4*      prim_alpha;    // per prim: consistent-normal alphas of a, b, c (or null)
     int                num_lights;
     float              light_area;
+    // bounding box of the emitter triangles and the margin that keeps every hit the
+    // traversal reports on an emitter inside it (emitter_span, estimator.cuh)
+    float3             light_lo, light_hi;
+    float              light_pad;
     int                env_w, env_h;
     float              env_norm;  // 1 / sum of sin-warped luminance
     int                num_prims;

@@ -82,6 +82,8 @@ def load_restatement():
         lib.orc_scene_set_tree.argtypes = [P, P, P, I, P, P, I]
         lib.orc_render.restype = LL
         lib.orc_render.argtypes = [P, P, P, ctypes.c_ulonglong, I, I, I, P, P, P, P, I, P, I, P]
+        lib.orc_last_extension_rays.restype = LL
+        lib.orc_last_extension_rays.argtypes = []
         lib.orc_trace.argtypes = [P, P, LL, I, P, P]
         lib.orc_material_sample.argtypes = [I, P, F, F, P, P, F, F, P, P, P]
         lib.orc_material_evaluate.argtypes = [I, P, F, F, P, P, P, P, P]
@@ -239,7 +241,7 @@ class OracleScene:
 
     def render(self, camera, width, height, spp, max_depth, rr_depth=-1, seed=0, rows=None, threads=None,
                keep_paths=False, dLdI=None, n_albedo=0, n_emission=0, ref_stream=0):
-        """Returns dict(mean, var_of_mean, rays, paths?, g_albedo?, g_emission?)."""
+        """Returns dict(mean, var_of_mean, rays, extension_rays, paths?, g_albedo?, g_emission?)."""
         r0, r1 = (0, height) if rows is None else rows
         threads = threads or os.cpu_count() or 1
         cam = np.ascontiguousarray(camera, np.float32)
@@ -254,7 +256,8 @@ class OracleScene:
                                    ptr(s2), ptr(paths), ptr(dl), n_albedo, ptr(ga), n_emission, ptr(ge))
         mean = s / spp
         var = np.maximum(s2 / spp - mean * mean, 0.0) / max(spp - 1, 1)
-        out = {"mean": mean, "var_of_mean": var, "rays": int(rays)}
+        out = {"mean": mean, "var_of_mean": var, "rays": int(rays),
+               "extension_rays": int(self.lib.orc_last_extension_rays())}
         if keep_paths:
             out["paths"] = paths
         if dl is not None:

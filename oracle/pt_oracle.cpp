@@ -197,6 +197,7 @@ struct RefStream
 // extension-ray log (debugging the replay): {path, n, ox, oy, oz, dx, dy, dz, prim, t}
 static std::vector<double> g_ray_log;
 static bool                g_ray_log_on = false;
+static std::atomic<long long> g_ext_rays(0);  // extension rays of the last orc_render call
 static long long           g_cur_path = 0;
 
 // Random numbers consumed per scattering vertex, in this order.
@@ -1077,6 +1078,7 @@ struct PathOut
 {
     V3<T>     L;
     long long rays = 0;
+    long long ext = 0;  // of which extension rays
 };
 
 // dL: adjoint seed for this path (dLoss/dI_px / spp); grads accumulate when non-null
@@ -1106,6 +1108,7 @@ PathOut<T> tracePath(const Scene<T>& sc, const V3<T>& o0, const V3<T>& d0, Pcg32
     {
         Hit<T> hit = sc.trace(ro, rd, eps, inf, false);
         out.rays++;
+        out.ext++;
         if (g_ray_log_on)
         {
             double rec[10] = {double(g_cur_path), double(n), double(ro.x), double(ro.y), double(ro.z),
@@ -1382,7 +1385,7 @@ long long renderRows(const RenderJob<T>& job, int row_begin, int row_end, int nt
     if (rs) nt = 1;  // one global stream, consumed in the reference's pixel order
     std::vector<std::vector<double>> tga(nt), tge(nt);
     auto worker = [&](int tid) {
-        long long myrays = 0;
+        long long myrays = 0, myext = 0;
         std::vector<double>* pa = nullptr;
         std::vector<double>* pe = nullptr;
         if (ga)
@@ -1431,6 +1434,7 @@ long long renderRows(const RenderJob<T>& job, int row_begin, int row_end, int nt
                     g_cur_path = static_cast<long long>(pix) * rp.spp + si;
                     PathOut<T> po = tracePath(*job.sc, o, d, rng, rp, job.dLdI ? &dl : nullptr, pa, pe, rs);
                     myrays += po.rays;
+                    myext += po.ext;
                     V3<T> v(fmaxr(T(0), po.L.x), fmaxr(T(0), po.L.y), fmaxr(T(0), po.L.z));
                     for (int c = 0; c < 3; ++c)
                     {
@@ -1454,6 +1458,7 @@ long long renderRows(const RenderJob<T>& job, int row_begin, int row_end, int nt
             }
         }
         rays += myrays;
+        g_ext_rays += myext;
     };
     std::vector<std::thread> th;
     for (int i = 1; i < nt; ++i) th.emplace_back(worker, i);
@@ -1653,6 +1658,7 @@ long long orc_render(void* h, const float* cam, const int* ip, unsigned long lon
                      double* g_albedo, int n_emis, double* g_emis)
 {
     SceneAny* s = static_cast<SceneAny*>(h);
+    g_ext_rays = 0;
     if (s->precision == 64)
         return renderT(*s->d, cam, ip, seed, row_begin, row_end, nthreads, sum, sumsq, paths, dLdI, n_albedo,
                        g_albedo, n_emis, g_emis);
@@ -1773,6 +1779,7 @@ void orc_envmap_sample_texel(void* h, float r1, float r2, int* ui, int* vi)
 }
 
 void orc_set_draw_log(long long* log) { g_draw_log = log; }
+long long orc_last_extension_rays() { return g_ext_rays.load(); }
 void orc_ray_log(int on) { g_ray_log_on = on != 0; g_ray_log.clear(); }
 long long orc_ray_log_size() { return static_cast<long long>(g_ray_log.size() / 10); }
 void orc_ray_log_read(double* out) { std::memcpy(out, g_ray_log.data(), sizeof(double) * g_ray_log.size()); }

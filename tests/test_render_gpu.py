@@ -20,6 +20,15 @@ def _crn_compare(gpu, cpu, name):
     assert mre < 5e-3, f"{name}: mean relative error {mre:.2e}"
 
 
+def _ray_counts_agree(st, ref):
+    """Same estimator, same random numbers: the same extension rays to within a few paths.
+    The oracle traces every next-event ray of the reference; the GPU skips the area-light
+    rays that cannot reach the emitters' box, so it traces at most as many."""
+    assert abs(st["extension_rays"] - ref["extension_rays"]) <= 0.01 * ref["extension_rays"]
+    ref_nee = ref["rays"] - ref["extension_rays"]
+    assert st["shadow_rays"] <= 1.01 * ref_nee
+
+
 @pytest.mark.parametrize("traverse", [0, 1])
 def test_cfg0_crn_matches_float_oracle(traverse, cuda_device):
     from mcrt_gb300 import GpuScene
@@ -28,8 +37,7 @@ def test_cfg0_crn_matches_float_oracle(traverse, cuda_device):
     gpu, st = GpuScene(desc).render(cam, spp=16, max_depth=8, rr_depth=3, seed=7, traverse=traverse)
     ref = OracleScene(desc, 32).render(cam.as_array(), 32, 32, 16, 8, 3, seed=7)
     _crn_compare(gpu, ref["mean"].astype(np.float32), "cfg0")
-    # same estimator, same random numbers: the same number of rays to within a few paths
-    assert abs(st["rays"] - ref["rays"]) <= 0.01 * ref["rays"]
+    _ray_counts_agree(st, ref)
 
 
 def test_cfg1_small_crn_matches_float_oracle(cuda_device):
@@ -325,7 +333,7 @@ def test_phong_crn_matches_float_oracle(cuda_device):
     gpu, st = GpuScene(desc).render(cam, spp=16, max_depth=8, rr_depth=3, seed=9)
     ref = OracleScene(desc, 32).render(cam.as_array(), 32, 32, 16, 8, 3, seed=9)
     _crn_compare(gpu, ref["mean"].astype(np.float32), "phong")
-    assert abs(st["rays"] - ref["rays"]) <= 0.01 * ref["rays"]
+    _ray_counts_agree(st, ref)
 
 
 def test_scene_built_through_the_mcrt_api_renders_the_same_image(cuda_device):
@@ -344,3 +352,30 @@ def test_scene_built_through_the_mcrt_api_renders_the_same_image(cuda_device):
     a, _ = sc.finalize().render(sc.camera(), spp=8, max_depth=10, seed=5)
     b, _ = GpuScene(desc).render(cam, spp=8, max_depth=10, seed=5)
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_emitter_box_culling_changes_no_pixel(schedule, cuda_device):
+    """Next-event rays toward the area lights are culled, bounded and cut short by the box
+    of the emitter triangles.  Two point-sized emitters far outside the scene widen that box
+    over everything, so nothing is culled, without changing how the lights are sampled:
+    they come first in the emitter CDF with probability 0 and are never hit.  The image is
+    the same to the bit; only the number of traced next-event rays differs."""
+    from mcrt_gb300 import TRAVERSE_FAST, TRAVERSE_REF, GpuScene, scenes
+    from mcrt_gb300.scene import LGHT, Material, SceneDesc
+    desc = scenes.cfg0_scene()
+    cam = scenes.cfg0_camera(48, 48)
+    mats = list(desc.materials) + [Material(LGHT, (0.0, 0.0, 0.0))]
+    far = np.array([[-50.0] * 9, [50.0] * 9], np.float32)
+    up = np.tile(np.array([0.0, 1.0, 0.0], np.float32), (2, 3))
+    wide = SceneDesc(np.concatenate([far, desc.vertices]),
+                     np.concatenate([np.full(2, len(mats) - 1), desc.material_ids]).astype(np.int32), mats,
+                     normals=np.concatenate([up, desc.normals]))
+    kw = dict(spp=32, max_depth=8, rr_depth=3, seed=21, schedule=schedule)
+    tight, loose = GpuScene(desc), GpuScene(wide)
+    for traverse in (TRAVERSE_FAST, TRAVERSE_REF):
+        a, sa = tight.render(cam, traverse=traverse, **kw)
+        b, sb = loose.render(cam, traverse=traverse, **kw)
+        np.testing.assert_array_equal(a, b)
+        assert sa["extension_rays"] == sb["extension_rays"]
+        assert sa["shadow_rays"] < 0.8 * sb["shadow_rays"], (sa["shadow_rays"], sb["shadow_rays"])
