@@ -45,12 +45,15 @@ __device__ __forceinline__ bool emitter_span(const SceneView& S, float3 o, float
 #pragma unroll
     for (int a = 0; a < 3; ++a)
     {
-        if (dd[a] == 0.f)
+        // an axis the ray moves along by less than 1e-20 per unit: parallel to the slab
+        // (another axis bounds t by the box, so the drift stays far inside the margin)
+        if (fabsf(dd[a]) < 1e-20f)
         {
             if (oo[a] < lo[a] || oo[a] > hi[a]) return false;
             continue;
         }
-        const float ta = (lo[a] - oo[a]) / dd[a], tb = (hi[a] - oo[a]) / dd[a];
+        const float inv = __fdividef(1.0f, dd[a]);  // within 2 ulp: far inside the margin
+        const float ta = (lo[a] - oo[a]) * inv, tb = (hi[a] - oo[a]) * inv;
         t0 = fmaxf(t0, fminf(ta, tb));
         t1 = fminf(t1, fmaxf(ta, tb));
     }

@@ -192,36 +192,54 @@ __global__ void k_iter_begin(WaveArgs a, int p)
     c->next += static_cast<unsigned long long>(n);
 }
 
-// Gradient accumulators of an adjoint launch: per block in shared memory (flushed with
-// one global atomic per nonzero entry when the block ends) or straight to the global
-// vectors when they do not fit.
+// Gradient accumulators of an adjoint launch.  A kernel adds to the albedo gradients
+// (GRAD_ALBEDO: k_regen, k_shade), to the emission gradients (GRAD_EMISSION: k_shade,
+// k_connect) or both; each part it adds to is kept per block in shared memory when
+// WaveArgs::grad_shared has that part's bit (flushed with one global atomic per nonzero
+// entry when the block ends), and goes straight to the global vector otherwise.  A kernel's
+// dynamic shared memory is the parts it uses (grad_smem_bytes), so the next-event kernels
+// hold no albedo slice and keep their occupancy when there are thousands of albedos.
+constexpr int GRAD_ALBEDO = 1, GRAD_EMISSION = 2;
+// A part is kept per block while it fits 20 KB: then k_shade and k_regen keep their 9
+// blocks per SM.  Few parameters need it (global atomics on cfg3's 256 albedos: adjoint
+// 127 ms instead of 11.8); many do better in global memory at full occupancy (cfg4's 4096
+// albedos, 48 KB: forward + adjoint 106.9 ms in global memory, 113.4 per block).
+#ifndef MCRT_GRAD_SHARED_MAX
+#define MCRT_GRAD_SHARED_MAX 20480
+#endif
+constexpr size_t kGradSharedMax = MCRT_GRAD_SHARED_MAX;  // bytes of one part kept per block
+
 struct Grads
 {
     float* ga;
     float* ge;
 };
 
-template <bool ADJ>
+template <bool ADJ, int PARTS>
 __device__ __forceinline__ Grads grads_begin(const WaveArgs& a, float* sgrad)
 {
     Grads g{a.g_albedo, a.g_emis};
-    if (ADJ && a.grad_shared)
-    {
-        const int ng = 3 * (a.n_albedo + a.n_emis);
-        for (int k = threadIdx.x; k < ng; k += blockDim.x) sgrad[k] = 0.f;
-        __syncthreads();
-        g.ga = sgrad;
-        g.ge = sgrad + 3 * a.n_albedo;
-    }
+    if (!ADJ) return g;
+    const bool sa = (PARTS & GRAD_ALBEDO) && (a.grad_shared & GRAD_ALBEDO);
+    const bool se = (PARTS & GRAD_EMISSION) && (a.grad_shared & GRAD_EMISSION);
+    if (!sa && !se) return g;  // uniform over the block: kernel arguments only
+    const int ng = (sa ? 3 * a.n_albedo : 0) + (se ? 3 * a.n_emis : 0);
+    for (int k = threadIdx.x; k < ng; k += blockDim.x) sgrad[k] = 0.f;
+    __syncthreads();
+    if (sa) g.ga = sgrad;
+    if (se) g.ge = sgrad + (sa ? 3 * a.n_albedo : 0);
     return g;
 }
 
-template <bool ADJ>
+template <bool ADJ, int PARTS>
 __device__ __forceinline__ void grads_end(const WaveArgs& a, const float* sgrad)
 {
-    if (!ADJ || !a.grad_shared) return;
+    if (!ADJ) return;
+    const bool sa = (PARTS & GRAD_ALBEDO) && (a.grad_shared & GRAD_ALBEDO);
+    const bool se = (PARTS & GRAD_EMISSION) && (a.grad_shared & GRAD_EMISSION);
+    if (!sa && !se) return;
     __syncthreads();
-    const int na = 3 * a.n_albedo, ng = 3 * (a.n_albedo + a.n_emis);
+    const int na = sa ? 3 * a.n_albedo : 0, ng = na + (se ? 3 * a.n_emis : 0);
     for (int k = threadIdx.x; k < ng; k += blockDim.x)
     {
         const float v = sgrad[k];
@@ -233,6 +251,15 @@ __device__ __forceinline__ void grads_end(const WaveArgs& a, const float* sgrad)
                 atomicAdd(&a.g_emis[k - na], v);
         }
     }
+}
+
+// dynamic shared memory of a kernel that adds to the gradient parts PARTS
+inline size_t grad_smem_bytes(const WaveArgs& a, int parts)
+{
+    size_t n = 0;
+    if ((parts & GRAD_ALBEDO) && (a.grad_shared & GRAD_ALBEDO)) n += 3 * static_cast<size_t>(a.n_albedo);
+    if ((parts & GRAD_EMISSION) && (a.grad_shared & GRAD_EMISSION)) n += 3 * static_cast<size_t>(a.n_emis);
+    return n * sizeof(float);
 }
 
 __device__ __forceinline__ void add_grad3(float* g, int idx, float3 v)
@@ -410,7 +437,7 @@ template <bool ADJ>
 __global__ void __launch_bounds__(128) k_regen(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];
-    const Grads        G = grads_begin<ADJ>(a, sgrad);
+    const Grads        G = grads_begin<ADJ, GRAD_ALBEDO>(a, sgrad);
     const Ctrl*        c = a.ctrl;
     const int          nd = min(c->dcount[p], static_cast<int>(a.capacity));
     const int          nn = c->new_count;
@@ -428,7 +455,7 @@ __global__ void __launch_bounds__(128) k_regen(WaveArgs a, int p)
     }
     for (int off = 16; off > 0; off >>= 1) fin += __shfl_down_sync(0xffffffffu, fin, off);
     if (lane == 0 && fin) atomicAdd(&a.ctrl->finished, fin);
-    grads_end<ADJ>(a, sgrad);
+    grads_end<ADJ, GRAD_ALBEDO>(a, sgrad);
 }
 
 // Work distribution of the traversal kernels over a queue of n entries: with batch
@@ -572,7 +599,7 @@ __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];
     __shared__ int s_base[16], s_perm[kShadeWindow];
-    const Grads G = grads_begin<ADJ>(a, sgrad);
+    const Grads G = grads_begin<ADJ, GRAD_ALBEDO | GRAD_EMISSION>(a, sgrad);
     const int n = min(a.ctrl->qcount[p], static_cast<int>(a.capacity));
     const int lane = threadIdx.x & 31;
     const int pn = p ^ 1;
@@ -764,7 +791,7 @@ __global__ void __launch_bounds__(128, 9) k_shade(WaveArgs a, int p)
         pos += 128;
         if (pos % kShadeWindow == 0) pos += (gridDim.x - 1) * kShadeWindow;
     }
-    grads_end<ADJ>(a, sgrad);
+    grads_end<ADJ, GRAD_ALBEDO | GRAD_EMISSION>(a, sgrad);
 }
 
 // Adjoint (ADJ): the emission derivative of each next-event contribution (the
@@ -799,7 +826,7 @@ __global__ void __launch_bounds__(kTraceBlock, (Q == 0 && MINB > 1) ? kAnyHitMin
 {
     extern __shared__ float sgrad[];
     __shared__ int stack[STACK * kTraceBlock];
-    const Grads    G = grads_begin<ADJ>(a, sgrad);
+    const Grads    G = grads_begin<ADJ, GRAD_EMISSION>(a, sgrad);
     int*           st = stack + threadIdx.x;
     TraceCount     cnt = {0u, 0u};
     const int      n = min(a.ctrl->scount[Q], static_cast<int>(a.shadow_cap));
@@ -816,7 +843,7 @@ __global__ void __launch_bounds__(kTraceBlock, (Q == 0 && MINB > 1) ? kAnyHitMin
         connect_result<ADJ>(a, G, p, Q, k, hit, h);
     }
     if (COUNT) flush_count(a.stats, 4, cnt);
-    grads_end<ADJ>(a, sgrad);
+    grads_end<ADJ, GRAD_EMISSION>(a, sgrad);
 }
 
 // ---------------------------------------------------------------------------
@@ -1258,8 +1285,12 @@ struct StageTimer
 // one iteration of parity p (six launches); stage timer slots: 0 begin + regen,
 // 1 extend, 2 shade, 3 connect
 template <int STACK, bool COUNT, int MINB, bool ADJ = false, bool REFM = true>
-void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, StageTimer* tm, size_t dyn = 0)
+void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, StageTimer* tm)
 {
+    // adjoint: each kernel's shared gradient slices (0 for the forward)
+    const size_t dr = ADJ ? grad_smem_bytes(a, GRAD_ALBEDO) : 0;
+    const size_t ds = ADJ ? grad_smem_bytes(a, GRAD_ALBEDO | GRAD_EMISSION) : 0;
+    const size_t dc = ADJ ? grad_smem_bytes(a, GRAD_EMISSION) : 0;
     auto beg = [&](int stg) {
         if (tm) tm->record(st, stg, true);
     };
@@ -1268,23 +1299,23 @@ void enqueue_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t 
     };
     beg(0);
     k_iter_begin<<<1, 1, 0, st>>>(a, p);
-    k_regen<ADJ><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+    k_regen<ADJ><<<ls.grid_regen, 128, dr, st>>>(a, p);
     end();
     beg(1);
     k_extend<STACK, COUNT, MINB, REFM><<<ls.grid_trace, kTraceBlock, 0, st>>>(a, p);
     end();
     beg(2);
     if (ls.lights == 1)
-        k_shade<ADJ, 1><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+        k_shade<ADJ, 1><<<ls.grid_shade, 128, ds, st>>>(a, p);
     else if (ls.lights == 2)
-        k_shade<ADJ, 2><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+        k_shade<ADJ, 2><<<ls.grid_shade, 128, ds, st>>>(a, p);
     else
-        k_shade<ADJ, 3><<<ls.grid_shade, 128, dyn, st>>>(a, p);
+        k_shade<ADJ, 3><<<ls.grid_shade, 128, ds, st>>>(a, p);
     end();
     beg(3);
-    k_connect<STACK, COUNT, MINB, ADJ, 0, REFM><<<ls.grid_any, kTraceBlock, dyn, st>>>(a, p);
+    k_connect<STACK, COUNT, MINB, ADJ, 0, REFM><<<ls.grid_any, kTraceBlock, dc, st>>>(a, p);
     // closest-hit next-event rays exist only where a job has area lights
-    if (ls.lights & 2) k_connect<STACK, COUNT, MINB, ADJ, 1, REFM><<<ls.grid_connect, kTraceBlock, dyn, st>>>(a, p);
+    if (ls.lights & 2) k_connect<STACK, COUNT, MINB, ADJ, 1, REFM><<<ls.grid_connect, kTraceBlock, dc, st>>>(a, p);
     end();
 }
 
@@ -1614,32 +1645,36 @@ int run_stream(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<
 // REFM = false when every job traverses in FAST mode; the shading build follows ls.lights
 // (the forward's specialisations)
 template <int STACK, bool REFM>
-void enqueue_adjoint_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st, size_t dyn)
+void enqueue_adjoint_iter(const WaveArgs& a, int p, const LaunchShape& ls, cudaStream_t st)
 {
-    enqueue_iter<STACK, false, kTraceMinBlocks, true, REFM>(a, p, ls, st, nullptr, dyn);
+    enqueue_iter<STACK, false, kTraceMinBlocks, true, REFM>(a, p, ls, st, nullptr);
 }
 
 template <int STACK, bool REFM>
-int adjoint_launch_shape(size_t dyn, LaunchShape& ls)
+int adjoint_launch_shape(const WaveArgs& a, LaunchShape& ls)
 {
-    const int d = static_cast<int>(dyn);
-    CK(cudaFuncSetAttribute(k_regen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
-    CK(cudaFuncSetAttribute(k_shade<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
-    CK(cudaFuncSetAttribute(k_shade<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
-    CK(cudaFuncSetAttribute(k_shade<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
+    const int dr = static_cast<int>(grad_smem_bytes(a, GRAD_ALBEDO));
+    const int ds = static_cast<int>(grad_smem_bytes(a, GRAD_ALBEDO | GRAD_EMISSION));
+    const int dc = static_cast<int>(grad_smem_bytes(a, GRAD_EMISSION));
+    CK(cudaFuncSetAttribute(k_regen<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dr));
+    CK(cudaFuncSetAttribute(k_shade<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ds));
+    CK(cudaFuncSetAttribute(k_shade<true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, ds));
+    CK(cudaFuncSetAttribute(k_shade<true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, ds));
     constexpr int B = kTraceMinBlocks;
-    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 0, REFM>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
-    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 1, REFM>, cudaFuncAttributeMaxDynamicSharedMemorySize, d));
+    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 0, REFM>, cudaFuncAttributeMaxDynamicSharedMemorySize, dc));
+    CK(cudaFuncSetAttribute(k_connect<STACK, false, B, true, 1, REFM>, cudaFuncAttributeMaxDynamicSharedMemorySize, dc));
     const int sms = num_sms();
-    int       occ_e = 0, occ_s = 0, occ_a = 0, occ_c = 0;
+    int       occ_e = 0, occ_s = 0, occ_a = 0, occ_c = 0, occ_r = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_extend<STACK, false, B, REFM>, kTraceBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<true, 3>, 128, dyn);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_connect<STACK, false, B, true, 0, REFM>, kTraceBlock, dyn);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_connect<STACK, false, B, true, 1, REFM>, kTraceBlock, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_shade<true, 3>, 128, ds);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_r, k_regen<true>, 128, dr);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_connect<STACK, false, B, true, 0, REFM>, kTraceBlock, dc);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_connect<STACK, false, B, true, 1, REFM>, kTraceBlock, dc);
     ls.grid_trace = sms * std::max(occ_e, 1);
     ls.grid_any = sms * std::max(occ_a, 1);
     ls.grid_connect = sms * std::max(occ_c, 1);
     ls.grid_shade = sms * std::max(occ_s, 1);
+    ls.grid_regen = sms * std::max(occ_r, 1);
     ls.grid_small = sms * 8;
     ls.block = 128;
     return MCRT_OK;
@@ -1694,9 +1729,9 @@ int adjoint_stream(Workspace& w, const std::vector<JobGPU>& jobs, int64_t total,
     a.g_emis = ge;
     a.n_albedo = na;
     a.n_emis = ne;
-    const size_t gbytes = sizeof(float) * 3 * static_cast<size_t>(na + ne);
-    a.grad_shared = gbytes <= 64 * 1024 ? 1 : 0;
-    const size_t dyn = a.grad_shared ? gbytes : 0;
+    // each gradient part per block in shared memory when it fits kGradSharedMax
+    a.grad_shared = (sizeof(float) * 3 * static_cast<size_t>(na) <= kGradSharedMax ? GRAD_ALBEDO : 0) |
+                    (sizeof(float) * 3 * static_cast<size_t>(ne) <= kGradSharedMax ? GRAD_EMISSION : 0);
     const bool   stack32 = bvh_depth + 2 < kSmallStack;
     bool         fast_only = true;
     int          lights = 0;
@@ -1706,21 +1741,21 @@ int adjoint_stream(Workspace& w, const std::vector<JobGPU>& jobs, int64_t total,
         lights |= (J.scene.env_w > 0 ? 1 : 0) | (J.scene.light_area > 0.f ? 2 : 0);
     }
     LaunchShape ls;
-    rc = stack32 ? (fast_only ? adjoint_launch_shape<kSmallStack, false>(dyn, ls)
-                              : adjoint_launch_shape<kSmallStack, true>(dyn, ls))
-                 : (fast_only ? adjoint_launch_shape<kStack, false>(dyn, ls)
-                              : adjoint_launch_shape<kStack, true>(dyn, ls));
+    rc = stack32 ? (fast_only ? adjoint_launch_shape<kSmallStack, false>(a, ls)
+                              : adjoint_launch_shape<kSmallStack, true>(a, ls))
+                 : (fast_only ? adjoint_launch_shape<kStack, false>(a, ls)
+                              : adjoint_launch_shape<kStack, true>(a, ls));
     if (rc) return rc;
     ls.fast_only = fast_only;
     ls.lights = lights == 0 ? 3 : lights;
     run.iter_launches = (ls.lights & 2) ? 6 : 5;
     auto iter = [&](cudaStream_t s2, int p, StageTimer*) {
         if (stack32)
-            fast_only ? enqueue_adjoint_iter<kSmallStack, false>(a, p, ls, s2, dyn)
-                      : enqueue_adjoint_iter<kSmallStack, true>(a, p, ls, s2, dyn);
+            fast_only ? enqueue_adjoint_iter<kSmallStack, false>(a, p, ls, s2)
+                      : enqueue_adjoint_iter<kSmallStack, true>(a, p, ls, s2);
         else
-            fast_only ? enqueue_adjoint_iter<kStack, false>(a, p, ls, s2, dyn)
-                      : enqueue_adjoint_iter<kStack, true>(a, p, ls, s2, dyn);
+            fast_only ? enqueue_adjoint_iter<kStack, false>(a, p, ls, s2)
+                      : enqueue_adjoint_iter<kStack, true>(a, p, ls, s2);
     };
     StageTimer timer;
     return stream_loop(w, a, total, max_depth, false, true, st, timer, run, iter);
@@ -1974,6 +2009,7 @@ LaunchShape launch_shape_variant(bool stack32, bool regcap, bool fast_only)
     ls.grid_any = sms * std::max(occ_a, 1);
     ls.grid_connect = ls.grid_trace;
     ls.grid_shade = sms * std::max(occ_s, 1);
+    ls.grid_regen = ls.grid_shade;
     ls.grid_small = sms * 8;
     ls.block = 128;
     return ls;

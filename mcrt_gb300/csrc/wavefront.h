@@ -129,7 +129,7 @@ constexpr int kAdjLog = 16;
 
 struct LaunchShape
 {
-    int grid_trace, grid_any, grid_connect, grid_shade, grid_small, block;  // grid_any: any-hit k_connect
+    int grid_trace, grid_any, grid_connect, grid_shade, grid_regen, grid_small, block;  // grid_any: any-hit k_connect
     bool fast_only = false;  // every job traverses in FAST mode: kernels built without the REF traversal
     int  lights = 3;         // light kinds of the jobs (1 environment, 2 area, 3 both): the k_shade build
 };

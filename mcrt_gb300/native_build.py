@@ -47,8 +47,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(LIB_DIR, exist_ok=True)
-    # MCRT_NVCC_DEFINES: extra -D options for all sources (e.g. -DMCRT_FAST_WIDE=0 builds the
-    # two-child FAST traversal); a change of them rebuilds everything
+    # MCRT_NVCC_DEFINES: extra -D options for all sources (e.g. -DMCRT_FAST_WIDE=1 builds the
+    # eight-child FAST traversal); a change of them rebuilds everything
     defines = os.environ.get("MCRT_NVCC_DEFINES", "").split()
     if any(not d.startswith("-D") for d in defines):
         raise ValueError("MCRT_NVCC_DEFINES takes -D options only")

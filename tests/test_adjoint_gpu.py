@@ -8,9 +8,9 @@ pytestmark = pytest.mark.gpu
 RES, SPP, DEPTH = 32, 16, 6
 
 
-def _setup(seed=3):
+def _setup(seed=3, groups=256):
     from mcrt_gb300 import GpuScene, scenes
-    desc, albedo, emission = scenes.cfg3_scene(param_seed=seed)
+    desc, albedo, emission = scenes.cfg3_scene(param_seed=seed, groups=groups)
     cam = scenes.cfg0_camera(RES, RES)
     return desc, cam, albedo, emission, GpuScene(desc)
 
@@ -156,11 +156,13 @@ def test_batched_adjoint_equals_sum_of_single_adjoints(cuda_device):
     assert st["paths"] == 32 * 32 * 8 + 24 * 20 * 4
 
 
-@pytest.mark.parametrize("path_chunk", [0, 512])
-def test_wavefront_adjoint_equals_per_path_replay(path_chunk, cuda_device):
+@pytest.mark.parametrize("path_chunk,groups", [(0, 256), (512, 256), (0, 2560)])
+def test_wavefront_adjoint_equals_per_path_replay(path_chunk, groups, cuda_device):
     """The wavefront replay (queues, vertex log, split albedo term) and the one-thread-per-
-    path replay compute the same derivative; they differ only in float summation order."""
-    desc, cam, albedo, emission, sc = _setup()
+    path replay compute the same derivative; they differ only in float summation order.
+    256 albedo groups are summed per block in shared memory, 2560 (30 KB) straight into
+    the global vector."""
+    desc, cam, albedo, emission, sc = _setup(groups=groups)
     rng = np.random.default_rng(8)
     dl = rng.normal(size=(RES, RES, 3)).astype(np.float32)
     ga_w, ge_w, st_w = sc.render_adjoint(cam, SPP, DEPTH, dl, albedo.shape[0], 1, seed=4, schedule=0,
