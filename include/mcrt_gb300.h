@@ -257,7 +257,10 @@ int mcrt_envmap_load_bin(const char* path, int32_t* width, int32_t* height, floa
 int mcrt_scene_desc_hash(const mcrt_scene_desc* desc, uint64_t* hash);
 int mcrt_scene_save(const mcrt_scene* scene, const char* path);
 int mcrt_scene_load(const char* path, uint64_t expected_hash, mcrt_scene** out_scene);
-/* Replace material colours (e.g. optimised albedos) without rebuilding the scene. */
+/* Replace material colours (e.g. optimised albedos) without rebuilding the scene.  The
+ * emitter set and consistent normals are fixed when the scene is built: a material that
+ * would become or stop being MCRT_MAT_LGHT, or ask for MCRT_MAT_CONSISTENT in a scene built
+ * without it, fails with MCRT_ERR_INVALID_ARGUMENT and changes nothing. */
 int mcrt_scene_set_materials(mcrt_scene* scene, int32_t num_materials, const mcrt_material* materials,
                              void* stream);
 /* Sizes of the device-resident scene: fast nodes, reference-layout nodes, triangle refs. */

@@ -1108,6 +1108,7 @@ struct mcrt_scene
     int                device = 0;
     int                num_materials = 0;
     MaterialGPU*       d_materials = nullptr;
+    std::vector<int32_t> mat_types;  // the uploaded materials' types (mcrt_scene_set_materials)
     std::vector<int64_t> array_bytes;  // bytes of each uploaded array, in upload order
     uint64_t             desc_hash = 0;  // of the description the scene was built from
     // error word and ray counter of the batch-trace calls on device buffers, one pair per
@@ -2123,6 +2124,7 @@ int scene_from_host(const HostScene& hs, int64_t num_tris, uint64_t desc_hash, m
     v.num_prims = static_cast<int>(num_tris);
     s->d_materials = const_cast<MaterialGPU*>(mt);
     s->num_materials = static_cast<int>(hs.materials.size());
+    for (const MaterialGPU& g : hs.materials) s->mat_types.push_back(g.type);
     s->fast_nodes = static_cast<int64_t>(hs.bvh.fast_nodes.size());
     s->ref_nodes = static_cast<int64_t>(hs.bvh.ref_nodes.size());
     s->refs = static_cast<int64_t>(hs.bvh.ref_prims.size());
@@ -2243,6 +2245,22 @@ int mcrt_scene_set_materials(mcrt_scene* s, int32_t n, const mcrt_material* m, v
 {
     if (!s || !m) return fail(MCRT_ERR_INVALID_ARGUMENT, "null scene or materials");
     if (n != s->num_materials) return fail(MCRT_ERR_INVALID_ARGUMENT, "material count differs from the scene's");
+    // the emitter table, its bounding box and the consistent-normal alphas are built with
+    // the scene: a material may not become or stop being an emitter, nor ask for consistent
+    // normals the scene was built without
+    for (int k = 0; k < n; ++k)
+    {
+        const int t = m[k].type, base = t & 0xff;
+        if ((t & ~(0xff | MCRT_MAT_CONSISTENT)) != 0 ||
+            (base != MCRT_MAT_LGHT && base != MCRT_MAT_DIFF && base != MCRT_MAT_SPEC && base != MCRT_MAT_REFR &&
+             base != MCRT_MAT_GLSY && base != MCRT_MAT_GGX))
+            return fail(MCRT_ERR_INVALID_ARGUMENT, "unknown material type");
+        if ((base == MCRT_MAT_LGHT) != ((s->mat_types[k] & 0xff) == MCRT_MAT_LGHT))
+            return fail(MCRT_ERR_INVALID_ARGUMENT, "a material may not become or stop being an emitter (the emitter "
+                                                   "table is built with the scene)");
+        if ((t & MCRT_MAT_CONSISTENT) && !s->view.prim_alpha)
+            return fail(MCRT_ERR_INVALID_ARGUMENT, "consistent normals need a scene built with them");
+    }
     std::vector<MaterialGPU> g(n);
     for (int k = 0; k < n; ++k)
     {
@@ -2258,6 +2276,7 @@ int mcrt_scene_set_materials(mcrt_scene* s, int32_t n, const mcrt_material* m, v
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     CK(cudaMemcpyAsync(s->d_materials, g.data(), sizeof(MaterialGPU) * n, cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
+    for (int k = 0; k < n; ++k) s->mat_types[k] = m[k].type;
     return MCRT_OK;
 }
 

@@ -95,8 +95,9 @@ struct WaveArgs
     // next-event results by parity: [4 i + s] for queue position i, [4 capacity + 4 j + s]
     // for finished-list position j
     float4* nev[2];
-    // next-event queues: [0] any-hit, [1] closest-hit; meta = {result index, type | light << 2,
-    // pixel, job}
+    // next-event queues: [0] any-hit, [1] closest-hit; origin + stop distance (so.w: a
+    // closest-hit ray stops at a nearer hit, emitter_span), direction + tmax, value,
+    // meta = {result index, type | light << 2, pixel, job}; tmin is kEpsRay for all
     float4* so[2];
     float4* sd[2];
     float4* sv[2];

@@ -375,10 +375,18 @@ class GpuScene:
         return ga[:n_albedo], ge[:n_emission], stats_dict(st)
 
     def set_materials(self, materials: list):
+        """mcrt_scene_set_materials: new colours and parameters for the scene's materials
+        (the emitter set and consistent normals stay as built; McrtError otherwise, and the
+        scene keeps its materials)."""
+        old = self.desc.materials
         self.desc.materials = list(materials)
-        arr = self.desc.c_materials()
-        N.check(self._lib.mcrt_scene_set_materials(self.handle, len(materials), arr, None),
-                "mcrt_scene_set_materials")
+        try:
+            arr = self.desc.c_materials()
+            N.check(self._lib.mcrt_scene_set_materials(self.handle, len(materials), arr, None),
+                    "mcrt_scene_set_materials")
+        except Exception:
+            self.desc.materials = old
+            raise
 
 
 def make_params(spp, max_depth, rr_depth=-1, seed=0, traverse=N.TRAVERSE_FAST, path_chunk=0, use_graph=False,

@@ -379,3 +379,30 @@ def test_emitter_box_culling_changes_no_pixel(schedule, cuda_device):
         np.testing.assert_array_equal(a, b)
         assert sa["extension_rays"] == sb["extension_rays"]
         assert sa["shadow_rays"] < 0.8 * sb["shadow_rays"], (sa["shadow_rays"], sb["shadow_rays"])
+
+
+def test_set_materials_keeps_the_emitter_set(cuda_device):
+    """New colours are taken without a rebuild; a change of the emitter set (built into the
+    light table and the emitter box) or a request for consistent normals the scene was built
+    without is refused and changes nothing."""
+    import copy
+    from mcrt_gb300 import GpuScene, McrtError, scenes
+    from mcrt_gb300.scene import CONSISTENT, DIFF, LGHT
+    desc = scenes.cfg0_scene()
+    sc = GpuScene(desc)
+    cam = scenes.cfg0_camera(16, 16)
+    before, _ = sc.render(cam, spp=4, max_depth=4, seed=1)
+    light = next(i for i, m in enumerate(desc.materials) if m.type == LGHT)
+    wall = next(i for i, m in enumerate(desc.materials) if m.type == DIFF)
+    for k, t in ((light, DIFF), (wall, LGHT), (wall, DIFF | CONSISTENT), (wall, 77)):
+        mats = copy.deepcopy(desc.materials)
+        mats[k].type = t
+        with pytest.raises(McrtError):
+            sc.set_materials(mats)
+    after, _ = sc.render(cam, spp=4, max_depth=4, seed=1)
+    np.testing.assert_array_equal(before, after)
+    mats = copy.deepcopy(desc.materials)
+    mats[wall].color = (0.2, 0.3, 0.4)
+    sc.set_materials(mats)
+    changed, _ = sc.render(cam, spp=4, max_depth=4, seed=1)
+    assert not np.array_equal(before, changed)
