@@ -2635,8 +2635,10 @@ static int adjoint_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_came
     aa.total_paths = total;
     aa.stats = w.stats;
     aa.err = w.err;
+    // the same bound as the wavefront's (one view of cfg4's scene with 4096 albedos, depth
+    // 16: 5.8 ms in global memory, 11.1 ms per block; cfg3's 256: 7.0 per block, 20.3 global)
     size_t gbytes = sizeof(float) * 3 * static_cast<size_t>(n_albedo + n_emis);
-    aa.shared_grads = gbytes <= 96 * 1024 ? 1 : 0;
+    aa.shared_grads = gbytes <= kGradSharedMax ? 1 : 0;
     size_t dyn = aa.shared_grads ? gbytes : 0;
     // the static traversal stack plus the gradient accumulators may exceed the 48 KB default
     CK(cudaFuncSetAttribute(k_adjoint<kStack>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dyn)));

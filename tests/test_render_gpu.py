@@ -406,3 +406,44 @@ def test_set_materials_keeps_the_emitter_set(cuda_device):
     sc.set_materials(mats)
     changed, _ = sc.render(cam, spp=4, max_depth=4, seed=1)
     assert not np.array_equal(before, changed)
+
+
+@pytest.mark.parametrize("w,h,spp,depth", [(1, 1, 1, 0), (3, 2, 1, 1), (7, 5, 3, 0), (16, 9, 2, 3)])
+def test_small_and_odd_frames_match_the_oracle(w, h, spp, depth, cuda_device):
+    """Frame edges: one pixel, odd sizes, one sample (no tent filter), depth 0 (the camera
+    hit and its next-event rays only).  Same random numbers: per pixel the same value up to
+    float rounding, and the same extension rays."""
+    from mcrt_gb300 import CameraDesc, GpuScene, scenes
+    from oracle.oracle import OracleScene
+    desc = scenes.cfg0_scene()
+    cam = CameraDesc(width=w, height=h, **scenes.CORNELL_CAMERA)
+    gpu, st = GpuScene(desc).render(cam, spp=spp, max_depth=depth, rr_depth=-1, seed=5)
+    ref = OracleScene(desc, 32).render(cam.as_array(), w, h, spp, depth, -1, seed=5)
+    assert gpu.shape == (h, w, 3)
+    close = np.isclose(gpu, ref["mean"], rtol=2e-3, atol=1e-4).all(axis=-1)
+    assert close.mean() >= (1.0 if w * h < 10 else 0.9), (gpu, ref["mean"])
+    assert st["paths"] == w * h * spp
+    assert abs(st["extension_rays"] - ref["extension_rays"]) <= max(1, 0.01 * ref["extension_rays"])
+
+
+@pytest.mark.parametrize("with_env", [False, True])
+def test_single_emitter_triangle_and_empty_background(with_env, cuda_device):
+    """The smallest scene: one emitter triangle.  Camera rays that hit its front face see
+    its radiance, rays that hit its back see nothing, and missed rays see black or, with
+    an environment map, the map; the GPU and the oracle agree pixel by pixel."""
+    from mcrt_gb300 import CameraDesc, GpuScene, scenes
+    from mcrt_gb300.scene import LGHT, Material, SceneDesc
+    from oracle.oracle import OracleScene
+    v = np.array([[-1.0, -1.0, 0.0, 1.0, -1.0, 0.0, 0.0, 1.0, 0.0]], np.float32)
+    env = scenes.sky_envmap(64, 32) if with_env else None
+    desc = SceneDesc(v, np.zeros(1, np.int32), [Material(LGHT, (2.0, 3.0, 4.0))], envmap=env)
+    for z in (3.0, -3.0):  # the face the camera sees: front, then back
+        cam = CameraDesc(origin=(0.0, 0.0, z), target=(0.0, 0.0, 0.0), width=12, height=12, fov_y=50.0)
+        gpu, _ = GpuScene(desc).render(cam, spp=2, max_depth=2, seed=3)
+        ref = OracleScene(desc, 32).render(cam.as_array(), 12, 12, 2, 2, -1, seed=3)
+        np.testing.assert_allclose(gpu, ref["mean"], rtol=2e-3, atol=1e-4)
+        lit = np.isclose(gpu, [2.0, 3.0, 4.0], rtol=1e-5).all(axis=-1)
+        assert lit.any() == (z > 0)
+        if not with_env:  # each of the 2 samples sees the radiance or nothing
+            frac = gpu / np.array([2.0, 3.0, 4.0], np.float32)
+            np.testing.assert_allclose(frac, np.round(frac * 2) / 2, atol=1e-6)
