@@ -289,7 +289,8 @@ def _timed(fn, reps=1):
 def bench_cfg2(args):
     """64 procedural scenes of uneven size: one batched wavefront against the same renders
     issued scene by scene (streaming per scene, and the wave schedule per scene).
-    --cfg2-part batched|sequential|waves runs one of the three alone (launch lists);
+    --cfg2-part batched|sequential|waves|paths runs one of them alone (launch lists); `paths`
+    is the plain GPU path tracer (MCRT_SCHEDULE_PATHS: one thread per path) scene by scene;
     --no-autotune keeps the library's default launch configuration."""
     import torch
     from mcrt_gb300 import GpuScene, autotune, render_batch, scenes
@@ -331,6 +332,10 @@ def bench_cfg2(args):
         for s, c, (_, _, p), o in zip(gs, cams, jobs, outs):
             s.render(c, out=o, schedule=1, **p)
 
+    def sequential_paths():  # the plain GPU path tracer: one thread per path, scene by scene
+        for s, c, (_, _, p), o in zip(gs, cams, jobs, outs):
+            s.render(c, out=o, schedule=2, **p)
+
     line = {"workload": "cfg2: 64 scenes, displaced icospheres 1k-500k T in Cornell shells, res {128..1024}^2, "
                         "spp 1..64, depth 4..16", "part": part, "schedule": args.schedule,
             "scene_setup_s": round(setup_s, 1),
@@ -352,9 +357,14 @@ def bench_cfg2(args):
         sequential_waves()
         tw, _ = _timed(sequential_waves, reps=args.steps)
         line["sequential_waves_ms"] = round(tw * 1e3, 2)
+    if part in ("all", "paths"):
+        sequential_paths()
+        tp, _ = _timed(sequential_paths, reps=args.steps)
+        line["sequential_paths_ms"] = round(tp * 1e3, 2)
     if part == "all":
         line.update({"speedup_batched_vs_sequential": round(line["sequential_ms"] / line["batched_ms"], 3),
                      "speedup_batched_vs_sequential_waves": round(line["sequential_waves_ms"] / line["batched_ms"], 3),
+                     "speedup_batched_vs_plain_paths": round(line["sequential_paths_ms"] / line["batched_ms"], 3),
                      "scene_cache_load_s": round(load_s, 2), "scene_cache_mb": round(cache_mb, 1)})
     print(json.dumps(line), flush=True)
 
@@ -455,7 +465,7 @@ def main():
     ap.add_argument("--path-chunk", type=int, default=0, help="path slots in flight (0: library default)")
     ap.add_argument("--variant", type=int, default=0, help="traversal kernel variant bits (0: default policy)")
     ap.add_argument("--autotune", action="store_true", help="pick path_chunk / variant with mcrt_autotune first")
-    ap.add_argument("--cfg2-part", default="all", choices=["all", "batched", "sequential", "waves"],
+    ap.add_argument("--cfg2-part", default="all", choices=["all", "batched", "sequential", "waves", "paths"],
                     help="cfg2: run the batched render, the per-scene renders or the per-scene wave renders alone")
     ap.add_argument("--no-autotune", action="store_true", help="cfg2: the library's default launch configuration")
     ap.add_argument("--quick", action="store_true",

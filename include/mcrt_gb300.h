@@ -171,6 +171,9 @@ typedef struct mcrt_render_params {
  *   before the next starts (the queues shrink with depth). */
 #define MCRT_SCHEDULE_STREAM 0
 #define MCRT_SCHEDULE_WAVES 1
+/* the plain GPU path tracer: one thread runs each path from the camera to its end (no
+ * queues); the wavefront's image up to a few ulp (the same paths, rays and arithmetic) */
+#define MCRT_SCHEDULE_PATHS 2
 
 /* variant 0 = default policy (STACK32 when the BVH is shallow enough, REGCAP);
  * MCRT_VARIANT_EXPLICIT | bits = exactly the given bits (for tuning) */

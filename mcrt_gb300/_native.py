@@ -39,6 +39,7 @@ TONEMAP_GAMMA = 0
 TONEMAP_REINHARD = 1
 SCHEDULE_STREAM = 0
 SCHEDULE_WAVES = 1
+SCHEDULE_PATHS = 2  # the plain GPU path tracer: one thread per path
 BUILD_SAH = 0
 BUILD_EXTERNAL = 1
 BUILD_SAH_SPLIT = 2

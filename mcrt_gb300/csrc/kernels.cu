@@ -847,6 +847,139 @@ __global__ void __launch_bounds__(kTraceBlock, (Q == 0 && MINB > 1) ? kAnyHitMin
 }
 
 // ---------------------------------------------------------------------------
+// MCRT_SCHEDULE_PATHS: the plain GPU path tracer.  One thread runs a path from the camera
+// to its end (rayTrace's loop, demo_pt.cpp:523-651, in one kernel: no queues, no sorting,
+// no compaction) and writes its radiance to ring[g - first]; k_resolve_paths then sums
+// each pixel's samples in sample order.  The path arithmetic is the wavefront's, in the
+// same order (each vertex adds its next-event results, the next its emission), so the
+// image is the wavefront's up to the compiler's choice of fused multiply-adds in either
+// kernel (a few ulp).
+// ---------------------------------------------------------------------------
+constexpr int kPathBlock = 64;
+
+template <int STACK>
+__global__ void __launch_bounds__(kPathBlock) k_paths(WaveArgs a, int64_t first, int64_t end)
+{
+    __shared__ int     stack[STACK * kPathBlock];
+    int*               st = stack + threadIdx.x;
+    const float        inf = __int_as_float(0x7f800000);
+    unsigned long long ext = 0, nee_rays = 0;
+    for (int64_t g = first + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < end;
+         g += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        const JobGPU&    J = a.jobs[find_job(a.jobs, a.num_jobs, g)];
+        const SceneView& S = J.scene;
+        const int64_t    local = g - J.path_offset;
+        const int        pixel = static_cast<int>(local / J.spp);
+        const int        s = static_cast<int>(local - static_cast<int64_t>(pixel) * J.spp);
+        const int        x = pixel % J.width, y = pixel / J.width;
+        Pcg              rng;
+        rng.seed(J.seed, static_cast<uint32_t>(pixel), static_cast<uint32_t>(s));
+        const float r1 = 2.f * rng.uniform();
+        const float r2 = 2.f * rng.uniform();
+        const float dx = J.spp > 1 ? tent(r1) : 0.f, dy = J.spp > 1 ? tent(r2) : 0.f;
+        float3      o, d;
+        camera_ray(J.cam, (static_cast<float>(x) + 0.5f + dx) / static_cast<float>(J.width),
+                   (static_cast<float>(y) + 0.5f + dy) / static_cast<float>(J.height), o, d);
+        float3 L = mk(0.f, 0.f, 0.f), T = mk(1.f, 1.f, 1.f);
+        bool   last_nee = false;
+        for (int depth = 0; depth <= J.max_depth; ++depth)
+        {
+            Hit        h;
+            const bool hit = trace_ray<false, STACK>(S, J.traverse, o, d, kEpsRay, inf, st, kPathBlock, h, a.err);
+            ++ext;
+            const bool no_direct = depth == 0 || !last_nee;
+            if (!hit)
+            {
+                L = L + miss_emission(S, d, T, no_direct);
+                break;
+            }
+            int    matid;
+            float3 ns = shading_normal(S, h.prim, h.u, h.v, matid);
+            Mat    m = load_mat(S, matid);
+            if (m.consistent) ns = consistent_normal(S, h.prim, h.u, h.v, -d, ns);
+            const float3 phit = o + d * h.t;
+            if (m.type == MAT_LGHT)
+            {
+                if (no_direct && dot3(d, ns) < 0.f) L = L + T * m.color;
+                break;
+            }
+            float u[NUM_DIMS];
+#pragma unroll 1
+            for (int k = 0; k < NUM_DIMS; ++k) u[k] = rng.uniform();
+            const float3 wi = -d;
+            const bool   nee_here = does_nee(m.type);
+            if (nee_here)
+            {
+                NeeRay    nee[4];
+                const int nn = make_nee(S, m, wi, ns, phit, T, u, nee);
+                for (int r = 0; r < nn; ++r)
+                {
+                    Hit        hs;
+                    const bool any = nee[r].type == NEE_ENV;
+                    const bool hh = any ? trace_ray<true, STACK>(S, J.traverse, phit, nee[r].d, kEpsRay, nee[r].tmax,
+                                                                 st, kPathBlock, hs, a.err)
+                                        : trace_ray<false, STACK, false, true, true>(S, J.traverse, phit, nee[r].d,
+                                                                                   kEpsRay, nee[r].tmax, st,
+                                                                                   kPathBlock, hs, a.err, nullptr,
+                                                                                   nee[r].tterm);
+                    ++nee_rays;
+                    float3 coef;
+                    int    emat;
+                    L = L + nee_contribution(S, nee[r].type, nee[r].light, nee[r].val, nee[r].d, hh, hs, coef, emat);
+                }
+            }
+            float3     T2, cdir;
+            const bool cont = continue_path(m, wi, ns, T, u, depth, J.max_depth, J.rr_depth, T2, cdir);
+            last_nee = nee_here;
+            if (!cont) break;
+            T = T2;
+            o = phit;
+            d = cdir;
+        }
+        a.ring[g - first] = make_float4(L.x, L.y, L.z, 0.f);
+    }
+    for (int off = 16; off > 0; off >>= 1)
+    {
+        ext += __shfl_down_sync(0xffffffffu, ext, off);
+        nee_rays += __shfl_down_sync(0xffffffffu, nee_rays, off);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        atomicAdd(&a.stats[0], ext);
+        atomicAdd(&a.stats[1], nee_rays);
+    }
+}
+
+// the pixels whose samples are paths [first, end): the sum in sample order of each
+// sample's radiance (NaN scrubbed, clamped at 0), times 1 / spp -- the arithmetic of the
+// wavefront's resolve (FrameBuffer::accumulatePixel + scale, film.cpp:204-260)
+__global__ void __launch_bounds__(128) k_resolve_paths(WaveArgs a, int64_t first, int64_t end)
+{
+    for (int64_t g = first + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < end;
+         g += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    {
+        const JobGPU& J = a.jobs[find_job(a.jobs, a.num_jobs, g)];
+        const int64_t local = g - J.path_offset;
+        if (local % J.spp != 0) continue;  // one thread per pixel: its first sample's
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+        for (int k = 0; k < J.spp; ++k)
+        {
+            float4 v = a.ring[g - first + k];
+            if (isnan3(xyz(v))) v = make_float4(0.f, 0.f, 0.f, 0.f);  // demo_pt.cpp:653
+            s0 += fmax_ref(0.f, v.x);                                  // demo_pt.cpp:703
+            s1 += fmax_ref(0.f, v.y);
+            s2 += fmax_ref(0.f, v.z);
+        }
+        const float scale = static_cast<float>(1.0 / J.spp);
+        float*      out = J.image + 3 * (local / J.spp);
+        out[0] = s0 * scale;
+        out[1] = s1 * scale;
+        out[2] = s2 * scale;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // path-replay adjoint (Vicini et al. 2021): each path is re-traced from its seed and
 // differentiated on the fly; nothing is taped, memory is O(pixels + parameters).
 // The radiance of a path is multilinear in the Lambert albedos and the emitter
@@ -1343,7 +1476,7 @@ int validate_job_impl(const mcrt_scene* s, const mcrt_camera* c, const mcrt_rend
         return fail(MCRT_ERR_INVALID_ARGUMENT, "unknown traversal mode");
     if (static_cast<int64_t>(c->width) * c->height > (int64_t(1) << 31) / 2)
         return fail(MCRT_ERR_INVALID_ARGUMENT, "image too large");
-    if (p->schedule != MCRT_SCHEDULE_STREAM && p->schedule != MCRT_SCHEDULE_WAVES)
+    if (p->schedule != MCRT_SCHEDULE_STREAM && p->schedule != MCRT_SCHEDULE_WAVES && p->schedule != MCRT_SCHEDULE_PATHS)
         return fail(MCRT_ERR_INVALID_ARGUMENT, "unknown schedule");
     if (p->reserved != 0) return fail(MCRT_ERR_INVALID_ARGUMENT, "reserved field must be 0");
     if (p->path_chunk < 0 || p->path_chunk > kMaxQueue)
@@ -1437,42 +1570,49 @@ int begin_run(Workspace& w, const std::vector<JobGPU>& jobs, int64_t capacity, i
     return MCRT_OK;
 }
 
+// Boundaries of chunks of at most `capacity` paths on pixel boundaries (a pixel larger than
+// the capacity gets a chunk of its own): table[k] .. table[k + 1] is chunk k.
+std::vector<int64_t> pixel_chunks(const std::vector<JobGPU>& jobs, const std::vector<int64_t>& pix_spp,
+                                  int64_t total, int64_t capacity)
+{
+    const int            num_jobs = static_cast<int>(jobs.size());
+    std::vector<int64_t> table;
+    table.push_back(0);
+    int64_t pos = 0;
+    int     j = 0;
+    while (pos < total)
+    {
+        int64_t end = std::min(total, pos + capacity);
+        while (j + 1 < num_jobs && jobs[j + 1].path_offset <= end - 1) ++j;
+        // job containing `end` (exclusive bound): round down to its pixel boundary
+        int jj = j;
+        while (jj + 1 < num_jobs && jobs[jj + 1].path_offset <= end) ++jj;
+        if (end < total)
+        {
+            int64_t local = end - jobs[jj].path_offset;
+            int64_t rounded = jobs[jj].path_offset + (local / pix_spp[jj]) * pix_spp[jj];
+            if (rounded <= pos)
+            {
+                // one pixel larger than the capacity: extend to its end
+                rounded = jobs[jj].path_offset + ((local + pix_spp[jj] - 1) / pix_spp[jj]) * pix_spp[jj];
+            }
+            end = rounded;
+        }
+        table.push_back(end);
+        pos = end;
+    }
+    return table;
+}
+
 // WAVES: waves of at most path_chunk paths, on pixel boundaries; each wave is admitted
 // whole and runs until its last path is finished before the next is admitted
 int run_waves(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<int64_t>& pix_spp, int64_t total,
               int max_depth, int64_t path_chunk, bool stack32, bool regcap, bool count, bool stages, bool graph,
               const LaunchShape& lsv, cudaStream_t st, StageTimer& timer, RunResult& run)
 {
-    const int num_jobs = static_cast<int>(jobs.size());
-    int64_t   capacity = path_chunk > 0 ? path_chunk : (int64_t(1) << 22);
+    int64_t capacity = path_chunk > 0 ? path_chunk : (int64_t(1) << 22);
     capacity = std::max<int64_t>(capacity, 64);
-    std::vector<int64_t> table;
-    table.push_back(0);
-    {
-        int64_t pos = 0;
-        int     j = 0;
-        while (pos < total)
-        {
-            int64_t end = std::min(total, pos + capacity);
-            while (j + 1 < num_jobs && jobs[j + 1].path_offset <= end - 1) ++j;
-            // job containing `end` (exclusive bound): round down to its pixel boundary
-            int jj = j;
-            while (jj + 1 < num_jobs && jobs[jj + 1].path_offset <= end) ++jj;
-            if (end < total)
-            {
-                int64_t local = end - jobs[jj].path_offset;
-                int64_t rounded = jobs[jj].path_offset + (local / pix_spp[jj]) * pix_spp[jj];
-                if (rounded <= pos)
-                {
-                    // one pixel larger than the capacity: extend to its end
-                    rounded = jobs[jj].path_offset + ((local + pix_spp[jj] - 1) / pix_spp[jj]) * pix_spp[jj];
-                }
-                end = rounded;
-            }
-            table.push_back(end);
-            pos = end;
-        }
-    }
+    const std::vector<int64_t> table = pixel_chunks(jobs, pix_spp, total, capacity);
     const int64_t num_chunks = static_cast<int64_t>(table.size()) - 1;
     int64_t       max_chunk = 0;
     for (int64_t k = 0; k < num_chunks; ++k) max_chunk = std::max(max_chunk, table[k + 1] - table[k]);
@@ -1516,6 +1656,46 @@ int run_waves(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<i
         CK(cudaGetLastError());
         CK(cudaEventRecord(run.e1, st));
     }
+    return MCRT_OK;
+}
+
+// PATHS: the plain path tracer, one thread per path (k_paths), over chunks of at most
+// path_chunk paths (default 64 M) on pixel boundaries, each chunk's pixels resolved by
+// k_resolve_paths from the chunk's per-path radiance (the ring array)
+int run_paths(Workspace& w, const std::vector<JobGPU>& jobs, const std::vector<int64_t>& pix_spp, int64_t total,
+              int64_t path_chunk, int bvh_depth, cudaStream_t st, RunResult& run)
+{
+    int64_t capacity = path_chunk > 0 ? path_chunk : kDefaultQueue;
+    capacity = std::max<int64_t>(capacity, 64);
+    const std::vector<int64_t> table = pixel_chunks(jobs, pix_spp, total, capacity);
+    const int64_t              num_chunks = static_cast<int64_t>(table.size()) - 1;
+    int64_t                    max_chunk = 0;
+    for (int64_t k = 0; k < num_chunks; ++k) max_chunk = std::max(max_chunk, table[k + 1] - table[k]);
+    if (max_chunk > kMaxQueue) return fail(MCRT_ERR_INVALID_ARGUMENT, "one pixel's samples exceed the queue limit");
+    WaveArgs a;
+    int      rc = begin_run(w, jobs, 0, max_chunk, num_chunks, st, run, a);
+    if (rc) return rc;
+    const bool stack32 = bvh_depth + 2 < kSmallStack;
+    int        occ = 0;
+    if (stack32)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_paths<kSmallStack>, kPathBlock, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_paths<kStack>, kPathBlock, 0);
+    const int grid = num_sms() * std::max(occ, 1), grid_resolve = num_sms() * 8;
+    run.waves = num_chunks;
+    run.launches = 2 * num_chunks;
+    run.extend_launches = num_chunks;
+    CK(cudaEventRecord(run.e0, st));
+    for (int64_t k = 0; k < num_chunks; ++k)
+    {
+        if (stack32)
+            k_paths<kSmallStack><<<grid, kPathBlock, 0, st>>>(a, table[k], table[k + 1]);
+        else
+            k_paths<kStack><<<grid, kPathBlock, 0, st>>>(a, table[k], table[k + 1]);
+        k_resolve_paths<<<grid_resolve, 128, 0, st>>>(a, table[k], table[k + 1]);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(run.e1, st));
     return MCRT_OK;
 }
 
@@ -1858,6 +2038,8 @@ int render_jobs(int num_jobs, mcrt_scene* const* scenes, const mcrt_camera* cams
     int         rc = p0.schedule == MCRT_SCHEDULE_WAVES
                          ? run_waves(w, jobs, pix_spp, total, max_depth, p0.path_chunk, stack32, regcap, count, stages,
                                      graph, lsv, st, timer, run)
+                     : p0.schedule == MCRT_SCHEDULE_PATHS
+                         ? run_paths(w, jobs, pix_spp, total, p0.path_chunk, bvh_depth, st, run)
                          : run_stream(w, jobs, pix_spp, total, max_depth, p0.path_chunk, stack32, regcap, count,
                                       stages, graph, lsv, st, timer, run);
     if (rc)
