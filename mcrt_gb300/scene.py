@@ -349,7 +349,8 @@ class GpuScene:
                        d_albedo=None, d_emission=None, schedule: int = N.SCHEDULE_STREAM, path_chunk: int = 0):
         """Path-replay adjoint; returns (d_albedo (n,3), d_emission (m,3), stats).
         Gradients are ADDED into d_albedo / d_emission when given.  schedule STREAM replays
-        the paths through the wavefront queues; WAVES replays each path in one thread."""
+        the paths through the wavefront queues; WAVES and PATHS replay each path in one
+        thread."""
         p = make_params(spp, max_depth, rr_depth, seed, traverse, path_chunk, False, schedule=schedule)
         cam = camera.to_c()
         st = N.RenderStats()
