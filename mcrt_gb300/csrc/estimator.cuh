@@ -27,7 +27,7 @@ struct NeeRay
     float4 val;
     int    type;
     int    light;
-    float  tterm;  // closest-hit rays: a hit nearer than this cannot be an emitter (-inf: none)
+    float  tterm;  // closest-hit rays: a hit nearer than this cannot be an emitter (unused by any-hit rays)
 };
 
 // The part [t0, t1] of the ray o + t d (d unit length) inside the bounding box of the
