@@ -581,6 +581,25 @@ def main():
     # payload + meta in, 16 B result out.  Both kernels launch once per iteration.
     _, sc_cnt = sc.render(cam, seed=0, out=out, profile=PROFILE_COUNT, **kw)
     nb = sc_cnt["node_bytes"]
+    # the same counts by bounce class: a depth-0 counting render of the same seeds traces
+    # the camera rays alone (and their vertices' next-event rays); the rest of the
+    # extension rays are the secondary ones
+    _, sc_prim = sc.render(cam, seed=0, out=out, profile=PROFILE_COUNT, **dict(kw, max_depth=0))
+
+    def per_ray(nodes, tris, rays):
+        return {"rays": int(rays), "nodes_per_ray": round(nodes / max(rays, 1), 2),
+                "tris_per_ray": round(tris / max(rays, 1), 2),
+                "bytes_per_ray": round((nb * nodes + 48 * tris) / max(rays, 1) + 48, 1)}
+    per_class = {
+        "primary": per_ray(sc_prim["ext_nodes"], sc_prim["ext_tris"], sc_prim["extension_rays"]),
+        "secondary": per_ray(sc_cnt["ext_nodes"] - sc_prim["ext_nodes"], sc_cnt["ext_tris"] - sc_prim["ext_tris"],
+                             sc_cnt["extension_rays"] - sc_prim["extension_rays"]),
+        "next_event": {**per_ray(sc_cnt["nee_nodes"], sc_cnt["nee_tris"], sc_cnt["shadow_rays"]),
+                       "bytes_per_ray": round((nb * sc_cnt["nee_nodes"] + 48 * sc_cnt["nee_tris"])
+                                              / max(sc_cnt["shadow_rays"], 1) + 80, 1)},
+        "note": "counting build (MCRT_PROFILE_COUNT), same seeds as the timed steps; bytes per ray as the "
+                "roofline's algorithmic bytes (ray in + hit or result out included)",
+    }
     ext_bytes = nb * sc_cnt["ext_nodes"] + 48 * sc_cnt["ext_tris"] + (32 + 16) * sc_cnt["extension_rays"]
     nee_bytes = nb * sc_cnt["nee_nodes"] + 48 * sc_cnt["nee_tris"] + (64 + 16) * sc_cnt["shadow_rays"]
     launches_per_render = max(extend_launches, 1)
@@ -671,6 +690,7 @@ def main():
                          "node_bytes": nb,
                          "nodes_per_ray": round(kern_nodes / max(kern_rays, 1), 2),
                          "tris_per_ray": round(kern_tris / max(kern_rays, 1), 2),
+                         "per_bounce_class": per_class,
                          "share_of_step": round(kern_ms / max(staged_frame_ms, 1e-9), 3),
                          "timing": f"CUDA events around every launch, {n_staged} untimed renders of the same seeds",
                          "second_kernel": {"kernel": other, "achieved": round(other_achieved, 1),
