@@ -85,6 +85,7 @@ def load_restatement():
         lib.orc_last_extension_rays.restype = LL
         lib.orc_last_extension_rays.argtypes = []
         lib.orc_trace.argtypes = [P, P, LL, I, P, P]
+        lib.orc_linear_trace.argtypes = [P, P, LL, P, P, I]
         lib.orc_material_sample.argtypes = [I, P, F, F, P, P, F, F, P, P, P]
         lib.orc_material_evaluate.argtypes = [I, P, F, F, P, P, P, P, P]
         lib.orc_fresnel.restype = F
@@ -264,6 +265,16 @@ class OracleScene:
             out["g_albedo"] = ga
             out["g_emission"] = ge
         return out
+
+    def linear_trace(self, rays: np.ndarray, threads: int | None = None):
+        """Closest hits of (n, 8) rays by testing every triangle (float scenes): the
+        reference's DebugMesh linear scan.  Returns (t, prim); misses have t = inf, prim -1."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        t = np.empty(n, np.float32)
+        p = np.empty(n, np.int32)
+        self.lib.orc_linear_trace(self.h, ptr(rays), n, ptr(t), ptr(p), threads or os.cpu_count() or 1)
+        return t, p
 
     def trace(self, rays: np.ndarray, any_hit: bool = False):
         rays = np.ascontiguousarray(rays, np.float32)

@@ -1688,6 +1688,56 @@ void orc_trace(void* h, const float* rays, long long n, int any, float* t_out, i
     }
 }
 
+// Closest hit by testing every triangle (no tree): DebugMesh::intersect
+// (splitbvh/debug_mesh.cpp:780-809), the linear-scan oracle of the reference's one
+// known-answer check (demo_splitbvh.cpp:194-238).  The reference's Moller-Trumbore
+// acceptance; a tie keeps the lower primitive index (the first found).  Rays as orc_trace;
+// `threads` host threads over the rays.
+void orc_linear_trace(void* h, const float* rays, long long n, float* t_out, int* prim_out, int threads)
+{
+    SceneAny* s = static_cast<SceneAny*>(h);
+    if (!s->f)  // a double-precision scene: nothing traced
+    {
+        for (long long i = 0; i < n; ++i)
+        {
+            t_out[i] = std::numeric_limits<float>::infinity();
+            prim_out[i] = -1;
+        }
+        return;
+    }
+    const auto&     tris = s->f->tris;
+    const long long nt = static_cast<long long>(tris.size());
+    auto            work = [&](long long begin, long long end) {
+        for (long long i = begin; i < end; ++i)
+        {
+            const float*    r = rays + 8 * i;
+            const V3<float> o = ld3<float>(r), d = ld3<float>(r + 4);
+            float           best = r[7];
+            int             prim = -1;
+            for (long long p = 0; p < nt; ++p)
+            {
+                float t, u, v;
+                if (mtIntersect(o, d, tris[p].a, tris[p].b, tris[p].c, t, u, v) && t > r[3] && t < best)
+                {
+                    best = t;
+                    prim = static_cast<int>(p);
+                }
+            }
+            t_out[i] = prim >= 0 ? best : std::numeric_limits<float>::infinity();
+            prim_out[i] = prim;
+        }
+    };
+    const int                nth = std::max(1, threads);
+    std::vector<std::thread> th;
+    const long long          chunk = (n + nth - 1) / nth;
+    for (int k = 0; k < nth; ++k)
+    {
+        const long long b = k * chunk, e = std::min(n, b + chunk);
+        if (b < e) th.emplace_back(work, b, e);
+    }
+    for (auto& t : th) t.join();
+}
+
 // ---- per-function entry points (float arithmetic, for pins against the reference)
 void orc_material_sample(int type, const float* color, float roughness, float ior, const float* wi, const float* nl,
                          float r1, float r2, float* wo, float* weight, float* pdf)

@@ -260,3 +260,26 @@ def test_consistent_normal_matches_reference():
         lib.orc_consistent_normal(*[O.ptr(r) for r in rows], float(u[i]), float(v[i]), O.ptr(o))
         got[i] = o
     np.testing.assert_array_equal(got, want)
+
+
+def test_linear_scan_matches_the_oracle_tree():
+    """The oracle's linear scan (the reference's DebugMesh rule) and its tree traversal give
+    the same closest hits on 20,000 random rays against 1000 random triangles."""
+    from mcrt_gb300.scene import DIFF, Material, SceneDesc
+    from oracle.oracle import OracleScene
+    rng = np.random.default_rng(3)
+    verts = rng.uniform(-1, 1, (1000, 9)).astype(np.float32)
+    orc = OracleScene(SceneDesc(verts, np.zeros(1000, np.int32), [Material(DIFF, (0.5, 0.5, 0.5))]), 32)
+    n = 20000
+    d = rng.uniform(-0.5, 0.5, (n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-1, 1, (n, 3))
+    rays[:, 3] = 1e-4
+    rays[:, 4:7] = d
+    rays[:, 7] = np.inf
+    t_lin, p_lin = orc.linear_trace(rays, threads=4)
+    t_bvh, p_bvh = orc.trace(rays)
+    assert np.array_equal(p_lin, p_bvh)
+    hit = p_lin >= 0
+    assert np.array_equal(t_lin[hit], t_bvh[hit]) and hit.mean() > 0.5

@@ -303,3 +303,36 @@ def test_ref_mode_bit_exact_at_1_3m_triangles(cfg1_hits, cuda_device):
         sc.close()
     finally:
         ref.ref_bvh_destroy(h)
+
+
+@pytest.mark.parametrize("traverse", [0, 1])
+def test_linear_scan_known_answer_1m_rays(traverse, cuda_device):
+    """The reference's own known-answer check at its full size (demo_splitbvh.cpp:194-238):
+    1,000,000 rays from U[-1,1]^3 in directions normalize(U[-0.5,0.5]^3) against 1000
+    random triangles, closest-hit t compared with a linear scan of every triangle
+    (DebugMesh::intersect, debug_mesh.cpp:780-809) by the reference's own rule |dt| < 1e-6
+    (checkEqual, demo_splitbvh.cpp:62-65; both missing counts as agreement).  On the
+    library's own tree, in REF and FAST traversal: the same triangle on every non-marginal
+    ray, and the reference's rule met on all but 1 in 10,000 rays."""
+    from mcrt_gb300 import GpuScene
+    from mcrt_gb300.scene import DIFF, Material, SceneDesc
+    from oracle.oracle import OracleScene
+    rng = np.random.default_rng(194238)
+    verts = rng.uniform(-1, 1, (1000, 9)).astype(np.float32)
+    desc = SceneDesc(verts, np.zeros(1000, np.int32), [Material(DIFF, (0.5, 0.5, 0.5))])
+    n = 1_000_000
+    d = rng.uniform(-0.5, 0.5, (n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-1, 1, (n, 3))
+    rays[:, 3] = 1e-4  # Ray::s_ray_epsilon = NUM_EPS_RAY (ray.cpp:8)
+    rays[:, 4:7] = d
+    rays[:, 7] = np.inf
+    t_lin, p_lin = OracleScene(desc, 32).linear_trace(rays)
+    out = GpuScene(desc).trace_closest(rays, traverse)
+    t_gpu, p_gpu = out[:, 0], out[:, 3].view(np.int32)
+    agree = ((p_lin < 0) & (p_gpu < 0)) | ((p_lin >= 0) & (p_gpu >= 0) & (np.abs(t_gpu - t_lin) < 1e-6))
+    assert (p_lin >= 0).mean() > 0.5
+    bad, marginal = classify(verts, rays, t_lin, p_lin, t_gpu, p_gpu)
+    assert not bad.any(), f"{bad.sum()} non-marginal mismatches, e.g. ray {np.argmax(bad)}"
+    assert (~agree).sum() <= n // 10000, f"{(~agree).sum()} of {n} rays outside |dt| < 1e-6"
