@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from conftest import golden
-from parity import TRAVERSE_SETS, classify, fixture_scene, fixture_tree
+from parity import TRAVERSE_SETS, classify, fixture_scene, fixture_tree, mt_terms
 
 FIXTURES = ["cornell", "cfg0", "sphere5", "debugmesh", "debugmesh_diag"]
 
@@ -312,8 +312,12 @@ def test_linear_scan_known_answer_1m_rays(traverse, cuda_device):
     random triangles, closest-hit t compared with a linear scan of every triangle
     (DebugMesh::intersect, debug_mesh.cpp:780-809) by the reference's own rule |dt| < 1e-6
     (checkEqual, demo_splitbvh.cpp:62-65; both missing counts as agreement).  On the
-    library's own tree, in REF and FAST traversal: the same triangle on every non-marginal
-    ray, and the reference's rule met on all but 1 in 10,000 rays."""
+    library's own tree, in REF and FAST traversal: the reference's rule met on all but 1 in
+    10,000 rays, and the same triangle on every non-marginal ray unless the two triangles'
+    hits (in double) lie within that same 1e-6.  Random triangles cross one another: a ray
+    near a crossing meets two of them at nearly the same t, and float Moller-Trumbore, whose
+    t is accurate to a few ulp of the coordinates (not of a small t), may order them either
+    way (1 ray in 10^6 here, 88 float ulp of t apart)."""
     from mcrt_gb300 import GpuScene
     from mcrt_gb300.scene import DIFF, Material, SceneDesc
     from oracle.oracle import OracleScene
@@ -334,5 +338,9 @@ def test_linear_scan_known_answer_1m_rays(traverse, cuda_device):
     agree = ((p_lin < 0) & (p_gpu < 0)) | ((p_lin >= 0) & (p_gpu >= 0) & (np.abs(t_gpu - t_lin) < 1e-6))
     assert (p_lin >= 0).mean() > 0.5
     bad, marginal = classify(verts, rays, t_lin, p_lin, t_gpu, p_gpu)
+    _, _, t_a = mt_terms(verts, p_lin, rays)
+    _, _, t_b = mt_terms(verts, p_gpu, rays)
+    tie = (p_lin >= 0) & (p_gpu >= 0) & (np.abs(t_a - t_b) < 1e-6)
+    bad &= ~tie
     assert not bad.any(), f"{bad.sum()} non-marginal mismatches, e.g. ray {np.argmax(bad)}"
     assert (~agree).sum() <= n // 10000, f"{(~agree).sum()} of {n} rays outside |dt| < 1e-6"
