@@ -2427,6 +2427,7 @@ int mcrt_scene_set_materials(mcrt_scene* s, int32_t n, const mcrt_material* m, v
 {
     if (!s || !m) return fail(MCRT_ERR_INVALID_ARGUMENT, "null scene or materials");
     if (n != s->num_materials) return fail(MCRT_ERR_INVALID_ARGUMENT, "material count differs from the scene's");
+    std::lock_guard<std::mutex> lock(s->mu);  // not while a render of this scene runs
     // the emitter table, its bounding box and the consistent-normal alphas are built with
     // the scene: a material may not become or stop being an emitter, nor ask for consistent
     // normals the scene was built without
