@@ -56,7 +56,7 @@ def mt_terms(verts: np.ndarray, prim: np.ndarray, rays: np.ndarray):
         qv = np.cross(tv, e1)
         v = np.sum(d * qv, axis=1) * inv
         t = np.sum(e2 * qv, axis=1) * inv
-    bmin = np.minimum(np.minimum(u, v), 1.0 - u - v)
+        bmin = np.minimum(np.minimum(u, v), 1.0 - u - v)  # NaN where det = 0 (never marginal)
     return np.abs(det), bmin, t
 
 
