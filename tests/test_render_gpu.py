@@ -123,18 +123,24 @@ def test_unknown_schedule_is_rejected(cuda_device):
         GpuScene(desc).render(cam, spp=1, max_depth=2, schedule=7)
 
 
-def test_batch_equals_individual_renders(cuda_device):
+@pytest.mark.parametrize("schedule", [0, 2])
+def test_batch_equals_individual_renders(schedule, cuda_device):
+    """A batch of uneven jobs renders each job's own image, in the streaming wavefront and
+    in the plain one-thread-per-path tracer (chunks of 300 paths that straddle jobs)."""
     from mcrt_gb300 import GpuScene, render_batch, scenes
     jobs = scenes.cfg2_jobs(n_scenes=3, seed=11, max_level=4)
     gs = [GpuScene(d) for d, _, _ in jobs]
     cams = [c for _, c, _ in jobs]
     for c in cams:
         c.width = c.height = 32
-    params = [p for _, _, p in jobs]
+    params = [dict(p, schedule=schedule, path_chunk=300 if schedule == 2 else 0) for _, _, p in jobs]
     outs, st = render_batch(gs, cams, params)
     for s, c, p, o in zip(gs, cams, params, outs):
         single, _ = s.render(c, **p)
-        np.testing.assert_allclose(o, single, rtol=1e-5, atol=1e-6)
+        if schedule == 2:
+            np.testing.assert_array_equal(o, single)
+        else:
+            np.testing.assert_allclose(o, single, rtol=1e-5, atol=1e-6)
 
 
 @pytest.mark.parametrize("schedule", [0, 1])
