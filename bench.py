@@ -640,10 +640,18 @@ def main():
     # launches of our kernels inside the timed region
     launches = st_last["kernel_launches"] * args.steps
 
-    trace_leg = adjoint = None
+    trace_leg = adjoint = plain = None
     if rank == 0 and not args.quick:
         trace_leg = incoherent_trace_leg(sc, dev)
         adjoint = adjoint_ratio_leg()
+        # the same frame with the plain GPU path tracer (one thread per path, no queues):
+        # what the wavefront buys on this workload
+        pkw = dict(kw, schedule=2)
+        sc.render(cam, seed=0, out=out, **pkw)
+        tp, (_, stp) = _timed(lambda: sc.render(cam, seed=1, out=out, **pkw), reps=2)
+        plain = {"ms_per_frame": round(tp * 1e3, 2), "mrays_s": round(stp["rays"] / tp / 1e6, 1),
+                 "wavefront_speedup": round(tp * 1e3 / (total_ms / args.steps), 3),
+                 "what": "MCRT_SCHEDULE_PATHS: one thread runs each path start to end, same paths and rays"}
 
     cpu = None
     fp64 = None
@@ -702,6 +710,7 @@ def main():
                                   "note": "untimed renders with an event pair around every launch"},
             "trace_incoherent": trace_leg,
             "adjoint_over_forward": adjoint,
+            "plain_path_tracer": plain,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
