@@ -818,10 +818,11 @@ __device__ __forceinline__ void connect_result(const WaveArgs& a, const Grads& G
 // Q = 0: the any-hit queue (rays to the environment); Q = 1: the bounded closest-hit
 // queue (rays to area lights).  One kernel per queue: the any-hit build needs no
 // closest-hit state, so it fits 56 registers without spills (both in one kernel spilled
-// 80 B; next-event stage 37.8 -> 37.5 ms per cfg1 frame) and runs capped at 48 registers
-// for 10 blocks per SM (kAnyHitMinBlocks; 36.5 ms).
+// 80 B; next-event stage 37.8 -> 37.5 ms per cfg1 frame) and runs capped at 40 registers
+// for 12 blocks per SM (kAnyHitMinBlocks; its adjoint build at 10, kAnyHitMinBlocksAdj).
 template <int STACK, bool COUNT, int MINB, bool ADJ, int Q, bool REFM = true>
-__global__ void __launch_bounds__(kTraceBlock, (Q == 0 && MINB > 1) ? kAnyHitMinBlocks : MINB)
+__global__ void __launch_bounds__(kTraceBlock,
+                                  (Q == 0 && MINB > 1) ? (ADJ ? kAnyHitMinBlocksAdj : kAnyHitMinBlocks) : MINB)
     k_connect(WaveArgs a, int p)
 {
     extern __shared__ float sgrad[];

@@ -40,13 +40,15 @@ constexpr int kSmallStack = 32;
 #define MCRT_TRACE_MIN_BLOCKS 9
 #endif
 constexpr int kTraceMinBlocks = MCRT_TRACE_MIN_BLOCKS;
-// The any-hit next-event kernel under MCRT_VARIANT_REGCAP: 48 registers, 10 blocks per SM.
-// Next-event stage per cfg1 frame: 9 blocks 37.5 ms, 10 blocks 36.5, 12 blocks (40
-// registers, spills) 38.8.
+// The any-hit next-event kernel under MCRT_VARIANT_REGCAP: 40 registers, 12 blocks per SM
+// (40 B of spills).  Next-event stage per cfg1 frame: 10 blocks (48 registers, no spills)
+// 33.96 ms, 12 blocks 32.53 (an earlier build, with tmin read from the queue and more
+// spills: 9 blocks 37.5, 10 blocks 36.5, 12 blocks 38.8).  Its adjoint build keeps 10.
 #ifndef MCRT_ANYHIT_MIN_BLOCKS
-#define MCRT_ANYHIT_MIN_BLOCKS 10
+#define MCRT_ANYHIT_MIN_BLOCKS 12
 #endif
 constexpr int kAnyHitMinBlocks = MCRT_ANYHIT_MIN_BLOCKS;
+constexpr int kAnyHitMinBlocksAdj = 10;
 constexpr int kMaxDepth = 62;
 constexpr int64_t kMaxQueue = int64_t(1) << 27;     // rays per queue (result indices stay in int)
 // Streaming schedule default: 64 M rays (49 GB of queues).  Per cfg1 frame (67 M paths):
